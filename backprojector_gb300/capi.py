@@ -1,0 +1,344 @@
+"""ctypes binding of the C ABI (include/backprojector_gb300.h, include/bpgb_synth.h).
+
+The shared library is built in-tree by `backprojector_gb300.build` (or
+`__graft_entry__.build()`); importing a function that needs it raises when it is
+missing -- there is no Python or CPU fallback for any compute call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libbpgb300.so"
+
+# Status codes (bpgb_status)
+OK = 0
+ERR_INVALID_ARGUMENT = -1
+ERR_CUDA = -2
+ERR_OUT_OF_MEMORY = -3
+ERR_TIMEOUT = -4
+ERR_UNSUPPORTED = -5
+ERR_NO_DEVICE = -6
+ERR_WINDOW = -7
+
+DTYPE_F32, DTYPE_F16, DTYPE_BF16, DTYPE_C64 = 0, 1, 2, 3
+ALGO_AUTO, ALGO_EXACT, ALGO_FAST = 0, 1, 2
+ACCUM_F32, ACCUM_KAHAN = 0, 1
+GEOMETRY_NAMES = {0: "generic", 1: "single_laser", 2: "exhaustive", 3: "confocal"}
+
+# numpy view of bpgb_pair / CameraLaserPair (camera first, 32 bytes)
+PAIR_DTYPE = np.dtype([("camera_point", "<f4", (3,)), ("laser_point", "<f4", (3,)),
+                       ("camera_wall", "<f4"), ("laser_wall", "<f4")])
+assert PAIR_DTYPE.itemsize == 32
+
+
+class Options(C.Structure):
+    _fields_ = [("algo", C.c_int32), ("h_dtype", C.c_int32), ("accum", C.c_int32),
+                ("h_pitch", C.c_uint32), ("h_scale", C.c_float), ("tile", C.c_int32),
+                ("pair_splits", C.c_int32), ("checked", C.c_int32), ("spin_limit", C.c_uint32),
+                ("reserved", C.c_int32 * 7)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("algo", C.c_int32), ("geometry", C.c_int32), ("num_lasers", C.c_uint64),
+                ("num_spads", C.c_uint64), ("tile", C.c_uint32 * 3), ("window", C.c_uint32),
+                ("chunk", C.c_uint32), ("stages", C.c_uint32), ("pair_splits", C.c_uint32),
+                ("grid", C.c_uint32), ("threads", C.c_uint32), ("smem_bytes", C.c_uint32),
+                ("scratch_bytes", C.c_uint64), ("updates", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["tile"] = list(self.tile)
+        d["algo"] = {1: "exact", 2: "fast"}.get(self.algo, str(self.algo))
+        d["geometry"] = GEOMETRY_NAMES.get(self.geometry, str(self.geometry))
+        return d
+
+
+class BackprojectorError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_U32 = C.POINTER(C.c_uint32)
+
+# name -> (restype, argtypes); every exported symbol of include/*.h
+SIGNATURES: dict[str, tuple] = {
+    "bpgb_abi_version": (C.c_int, []),
+    "bpgb_status_string": (C.c_char_p, [C.c_int]),
+    "bpgb_last_error": (C.c_char_p, []),
+    "bpgb_options_default": (None, [C.POINTER(Options)]),
+    "bpgb_launch_count": (C.c_uint64, []),
+    "bpgb_backproject_f32": (C.c_int, [_P, C.c_uint64, C.c_uint32, _P, C.c_uint64, _P, _U32, _F,
+                                       _F, C.c_float, C.c_float]),
+    "bpgb_backproject_c64": (C.c_int, [_P, C.c_uint64, C.c_uint32, _P, C.c_uint64, _P, _U32, _F,
+                                       _F, C.c_float, C.c_float]),
+    "bpgb_backproject_host": (C.c_int, [_P, C.c_uint64, C.c_uint32, _P, C.c_uint64, _P, _U32, _F,
+                                        _F, C.c_float, C.c_float, C.POINTER(Options)]),
+    "bpgb_plan_create": (C.c_int, [C.POINTER(_P), _P, C.c_uint64, C.c_uint32, _U32, _F, _F,
+                                   C.c_float, C.c_float, C.POINTER(Options)]),
+    "bpgb_plan_execute": (C.c_int, [_P, _P, _P, _P]),
+    "bpgb_plan_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "bpgb_plan_get_info": (C.c_int, [_P, C.POINTER(PlanInfo)]),
+    "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
+    "bpgb_plan_destroy": (C.c_int, [_P]),
+    "bpgb_diag_wait_timeout": (C.c_int, [C.c_uint32]),
+    "bpgb_phasor_pulse": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
+                                    C.c_uint32, _P, C.c_uint32, _P]),
+    "bpgb_phasor_taps": (C.c_int, [C.c_float, C.c_float, C.c_uint32, _F, C.c_int]),
+    "bpgb_precompute_pairs": (C.c_int, [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
+                                        C.c_uint32, C.c_int, _P]),
+    "bpgb_volume_basis": (C.c_int, [_F, _F, _U32, _F, _F, _F]),
+    "bpgb_time_limits": (C.c_int, [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
+                                   C.c_uint32, _F, _F, C.c_float, C.c_float, _F, _F]),
+    "bpgb_backproject_capture": (C.c_int, [_F, C.c_uint32, _F, C.c_uint32, C.c_uint32, _F,
+                                           C.c_uint32, C.c_uint32, _F, _F, C.c_float, C.c_float,
+                                           C.c_int, _F, _F, _U32, _F, C.c_int,
+                                           C.POINTER(Options), _F]),
+    "bpgb_phasor_capture": (C.c_int, [_F, C.c_uint32, _F, C.c_uint32, C.c_uint32, _F, C.c_uint32,
+                                      C.c_uint32, _F, _F, C.c_float, C.c_float, C.c_int, _F, _F,
+                                      _U32, _F, C.c_float, C.POINTER(Options), _F]),
+    "bpgb_synth_render": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_float, C.c_float, _F, _F,
+                                    C.c_uint64, _F]),
+    "bpgb_synth_poisson": (C.c_int, [_F, C.c_uint64, C.c_float, C.c_uint64]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libbpgb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA extension first "
+                               "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    if status != OK:
+        L = lib()
+        msg = L.bpgb_last_error().decode(errors="replace")
+        name = L.bpgb_status_string(status).decode()
+        raise BackprojectorError(status, f"{what}: {name} ({status}): {msg}")
+
+
+def fptr(a: np.ndarray):
+    return a.ctypes.data_as(_F)
+
+
+def u32ptr(a: np.ndarray):
+    return a.ctypes.data_as(_U32)
+
+
+def vptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+def f32(a, shape=None) -> np.ndarray:
+    out = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if shape is not None and out.shape != tuple(shape):
+        out = out.reshape(shape)
+    return out
+
+
+def options(**kw) -> Options:
+    o = Options()
+    lib().bpgb_options_default(C.byref(o))
+    for k, v in kw.items():
+        if v is None:
+            continue
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def launch_count() -> int:
+    return int(lib().bpgb_launch_count())
+
+
+# ---------------------------------------------------------------- host helpers (no GPU)
+
+def volume_basis(volume_position, volume_size, voxels_per_side, wall_normal=(0, 0, 0)):
+    """(volume_zero_pos[3], voxel_inc[9]) as the reference computes them."""
+    pos, size, wn = f32(volume_position), f32(volume_size), f32(wall_normal)
+    n = np.ascontiguousarray(np.asarray(voxels_per_side, dtype=np.uint32))
+    zero = np.zeros(3, np.float32)
+    inc = np.zeros(9, np.float32)
+    check(lib().bpgb_volume_basis(fptr(pos), fptr(size), u32ptr(n), fptr(wn), fptr(zero), fptr(inc)),
+          "bpgb_volume_basis")
+    return zero, inc
+
+
+def time_limits(laser_position, laser_grid, camera_position, camera_grid, volume_position,
+                volume_size, t0, deltaT):
+    lg, cg = f32(laser_grid), f32(camera_grid)
+    mn, mx = C.c_float(), C.c_float()
+    check(lib().bpgb_time_limits(fptr(f32(laser_position)), fptr(lg), lg.shape[0], lg.shape[1],
+                                 fptr(f32(camera_position)), fptr(cg), cg.shape[0], cg.shape[1],
+                                 fptr(f32(volume_position)), fptr(f32(volume_size)), t0, deltaT,
+                                 C.byref(mn), C.byref(mx)), "bpgb_time_limits")
+    return mn.value, mx.value
+
+
+def phasor_taps(wavelength: float, deltaT: float, times: int = 4) -> np.ndarray:
+    """(2, K) array: cos taps then sin taps."""
+    K = lib().bpgb_phasor_taps(wavelength, deltaT, times, None, 0)
+    if K <= 0:
+        return np.zeros((2, 0), np.float32)
+    taps = np.zeros(2 * K, np.float32)
+    lib().bpgb_phasor_taps(wavelength, deltaT, times, fptr(taps), K)
+    return taps.reshape(2, K)
+
+
+def synth_render(pairs: np.ndarray, T: int, t0: float, deltaT: float, points, albedo) -> np.ndarray:
+    pts, alb = f32(points), f32(albedo)
+    out = np.empty((len(pairs), T), np.float32)
+    check(lib().bpgb_synth_render(vptr(pairs), len(pairs), T, t0, deltaT, fptr(pts), fptr(alb),
+                                  len(alb), fptr(out)), "bpgb_synth_render")
+    return out
+
+
+def synth_poisson(H: np.ndarray, peak: float, seed: int) -> np.ndarray:
+    assert H.dtype == np.float32 and H.flags.c_contiguous
+    check(lib().bpgb_synth_poisson(fptr(H), H.size, peak, seed), "bpgb_synth_poisson")
+    return H
+
+
+# ---------------------------------------------------------------- GPU calls (host buffers)
+
+def backproject_host(H: np.ndarray, pairs: np.ndarray, voxels_per_side, zero, inc, t0: float,
+                     deltaT: float, **opt) -> np.ndarray:
+    """bpgb_backproject_host: H [P, T] float32 (or complex64) on the host."""
+    P = len(pairs)
+    cplx = np.iscomplexobj(H)
+    Hc = np.ascontiguousarray(H, dtype=np.complex64 if cplx else None)
+    T = Hc.shape[-1]
+    n = np.ascontiguousarray(np.asarray(voxels_per_side, dtype=np.uint32))
+    out = np.zeros(tuple(int(x) for x in n), np.complex64 if cplx else np.float32)
+    if "h_dtype" not in opt:
+        opt["h_dtype"] = DTYPE_C64 if cplx else DTYPE_F32
+    o = options(**opt)
+    check(lib().bpgb_backproject_host(vptr(Hc), P * T, T, vptr(pairs), P, vptr(out), u32ptr(n),
+                                      fptr(f32(zero)), fptr(f32(inc)), t0, deltaT, C.byref(o)),
+          "bpgb_backproject_host")
+    return out
+
+
+def precompute_pairs(laser_position, laser_grid, camera_position, camera_grid, confocal=False):
+    cg = f32(camera_grid)
+    cx, cy = cg.shape[0], cg.shape[1]
+    if confocal:
+        lg = cg
+        lx = ly = 0
+        P = cx * cy
+    else:
+        lg = f32(laser_grid)
+        lx, ly = lg.shape[0], lg.shape[1]
+        P = lx * ly * cx * cy
+    out = np.zeros(P, PAIR_DTYPE)
+    check(lib().bpgb_precompute_pairs(fptr(f32(laser_position)), fptr(lg), lx, ly,
+                                      fptr(f32(camera_position)), fptr(cg), cx, cy,
+                                      1 if confocal else 0, vptr(out)), "bpgb_precompute_pairs")
+    return out
+
+
+# ---------------------------------------------------------------- plans (device buffers)
+
+def _ptr(x) -> C.c_void_p:
+    """Device pointer of a torch tensor or an int address."""
+    if x is None:
+        return C.c_void_p(0)
+    if hasattr(x, "data_ptr"):
+        return C.c_void_p(x.data_ptr())
+    return C.c_void_p(int(x))
+
+
+def _stream_ptr(stream) -> C.c_void_p:
+    if stream is None:
+        return C.c_void_p(0)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class Plan:
+    """bpgb_plan: geometry analysed once, execute() on device buffers (async)."""
+
+    def __init__(self, pairs: np.ndarray, T: int, voxels_per_side, zero, inc, t0: float,
+                 deltaT: float, **opt):
+        self._pairs = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+        self.n = tuple(int(v) for v in voxels_per_side)
+        n = np.asarray(self.n, dtype=np.uint32)
+        self.T = int(T)
+        self.opt = options(**opt)
+        h = C.c_void_p()
+        check(lib().bpgb_plan_create(C.byref(h), vptr(self._pairs), len(self._pairs), self.T,
+                                     u32ptr(n), fptr(f32(zero)), fptr(f32(inc)), t0, deltaT,
+                                     C.byref(self.opt)), "bpgb_plan_create")
+        self.handle = h
+
+    @property
+    def num_pairs(self) -> int:
+        return len(self._pairs)
+
+    def info(self) -> dict:
+        i = PlanInfo()
+        check(lib().bpgb_plan_get_info(self.handle, C.byref(i)), "bpgb_plan_get_info")
+        return i.as_dict()
+
+    def execute(self, d_H, d_volume, stream=None) -> None:
+        check(lib().bpgb_plan_execute(self.handle, _ptr(d_H), _ptr(d_volume), _stream_ptr(stream)),
+              "bpgb_plan_execute")
+
+    def check(self) -> int:
+        v = C.c_uint64()
+        check(lib().bpgb_plan_check(self.handle, C.byref(v)), "bpgb_plan_check")
+        return int(v.value)
+
+    def check_status(self) -> tuple[int, int]:
+        """(status, violations) without raising."""
+        v = C.c_uint64()
+        st = lib().bpgb_plan_check(self.handle, C.byref(v))
+        return st, int(v.value)
+
+    def dump_bins(self, voxel_ids, d_bins, stream=None) -> None:
+        ids = np.ascontiguousarray(np.asarray(voxel_ids, dtype=np.int64))
+        check(lib().bpgb_plan_dump_bins(self.handle, ids.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        len(ids), _ptr(d_bins), _stream_ptr(stream)),
+              "bpgb_plan_dump_bins")
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bpgb_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def phasor_pulse_device(d_H, rows: int, T: int, in_pitch: int, wavelength: float, deltaT: float,
+                        d_out, out_pitch: int, times: int = 4, stream=None) -> None:
+    check(lib().bpgb_phasor_pulse(_ptr(d_H), rows, T, in_pitch, wavelength, deltaT, times,
+                                  _ptr(d_out), out_pitch, _stream_ptr(stream)), "bpgb_phasor_pulse")

@@ -1,0 +1,869 @@
+// Factored, TMA-staged dense backprojection for sm_103a.
+//
+// Same quantity as the reference kernel (backproject_cuda.cu:117-175):
+//   V[v] = sum_p H[p, round((lw_p + |l_p - v| + |v - c_p| + cw_p - t0) / dT)]
+// restricted to in-range bins, for pair lists that factor as p = l * S + s (the
+// exhaustive and single-laser orders of precompute_distances, backproject.hpp:374-397)
+// or are confocal (:399-413, laser point = camera point, d = 2|v - c| + 2 cw).
+//
+// Work decomposition
+//   * A CTA owns one voxel tile (tdim = lane layout x warp layout, K voxels per thread
+//     along z) and, when `splits` > 1, a contiguous range of (laser, SPAD-chunk) items.
+//   * Warp 0 is the producer.  For every item it computes, per SPAD row of the chunk,
+//     the range of bins the tile can reach (exact distance bounds from the SPAD and
+//     the laser point to the tile's box), aligns it for TMA, writes a row record
+//     (SPAD position relative to the tile centre in bin units, row constant) and
+//     issues 2-D TMA tile loads of H[p, lo : lo + W] into a shared-memory stage.  Out-
+//     of-range bins (< 0 or >= T) arrive as zeros from the TMA unit, which is exactly
+//     the reference's "skip out-of-range bins" rule.
+//   * Warps 1..n are consumers.  Each thread keeps K voxels in registers: the laser leg
+//     A_k = |v_k - l| / dT + lw / dT - t0 / dT (recomputed per laser), the voxel's
+//     coordinates relative to the tile centre (bin units) and the K accumulators.  Per
+//     row and voxel:  q = |v - c|^2 (2 ops), rsqrt (MUFU), x = q * rsqrt(q) + A_k,
+//     + row constant, + 1.5*2^23 (round to nearest), gather from shared memory at
+//     the rounded index, accumulate (9 issue slots; FP16/BF16 rows use the one-op
+//     mixed-precision add).
+//   * Stages are handed over with mbarriers (full: TMA bytes + producer arrive; empty:
+//     one arrive per consumer warp).  Every wait is bounded; a wait that gives up sets
+//     an error counter the host reads (bpgb_plan_check) and the CTA drains its own
+//     in-flight copies before returning.
+//
+// Numerics: FP32 geometry relative to the tile centre, rsqrt.approx; FP32 or Kahan-
+// folded chunk sums.  Rounding is round-half-even instead of the reference's half-away
+// (ties need an exact .5 in FP32 and are measured with the mis-binned fraction).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bpgb_device.cuh"
+#include "bpgb_internal.h"
+
+namespace bpgb {
+
+namespace {
+
+constexpr uint32_t kMaxChunk = 32;
+constexpr uint32_t kTableBytes = kMaxChunk * 16;  // float4 per row
+constexpr float kMargin = 2.0f;                   // bins of slack around each window
+constexpr float kQEps = 1e-6f;                    // keeps q > 0 (bins^2)
+
+struct FastArgs {
+    uint32_t n[3];      // voxels per side
+    uint32_t tiles[3];  // tiles per axis
+    uint32_t tdim[3];   // tile size in voxels
+    uint32_t lane[3];   // lane layout (product 32)
+    uint32_t warp[3];   // consumer warp layout
+    float h[3];         // voxel step length along each frame axis (m)
+    float hs[3];        // h * sb (bins)
+    float sb;           // SPAD-leg scale: 1/dT (2/dT confocal)
+    float sa;           // laser-leg scale: 1/dT (0 confocal)
+    uint32_t W;         // staged bins per row
+    uint32_t BW;        // TMA box width (elements)
+    uint32_t nbox;      // boxes per row
+    uint32_t row_bytes; // shared bytes per row (W * esz)
+    uint32_t chunk;     // rows per stage
+    uint32_t stages;
+    uint32_t stage_bytes;
+    uint32_t align;     // TMA x alignment (elements)
+    uint64_t L, S;
+    uint32_t nchunks;   // ceil(S / chunk)
+    uint32_t splits;
+    uint32_t spin_limit;
+    uint32_t T;
+    float out_scale;
+    uint64_t nvox;
+};
+
+struct TileGeo {
+    uint32_t org[3];
+    float ctr[3];  // tile centre in voxel-index units
+};
+
+__device__ __forceinline__ void tile_of_block(const FastArgs &a, uint32_t tile, TileGeo &g) {
+    const uint32_t tz = tile % a.tiles[2];
+    tile /= a.tiles[2];
+    const uint32_t tx = tile % a.tiles[0];
+    const uint32_t ty = tile / a.tiles[0];
+    g.org[0] = tx * a.tdim[0];
+    g.org[1] = ty * a.tdim[1];
+    g.org[2] = tz * a.tdim[2];
+#pragma unroll
+    for (int k = 0; k < 3; k++) g.ctr[k] = __fmaf_rn(0.5f, (float)(a.tdim[k] - 1), (float)g.org[k]);
+}
+
+// Distance bounds from point p (frame coordinates, metres) to the tile's box of voxel
+// centres: min to the clamped point, max to the farthest corner.
+__device__ __forceinline__ void box_bounds(const FastArgs &a, const TileGeo &g, float px,
+                                           float py, float pz, float &dmin, float &dmax) {
+    const float p[3] = {px, py, pz};
+    float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float lo = __fmul_rn((float)g.org[k], a.h[k]);
+        const float hi = __fmul_rn((float)(g.org[k] + a.tdim[k] - 1), a.h[k]);
+        const float c = fminf(fmaxf(p[k], lo), hi);
+        const float d0 = p[k] - c;
+        const float e0 = p[k] - lo, e1 = p[k] - hi;
+        s0 = __fmaf_rn(d0, d0, s0);
+        s1 = __fadd_rn(s1, fmaxf(__fmul_rn(e0, e0), __fmul_rn(e1, e1)));
+    }
+    dmin = sqrtf(s0);
+    dmax = sqrtf(s1);
+}
+
+// Row record of SPAD entry G (frame position, row constant Cs) for a tile and laser Lt:
+// e = (c' relative to the tile centre in bin units, Cs - lo); returns lo (the window's
+// first bin, aligned down to a.align).
+__device__ __forceinline__ int32_t row_record(const FastArgs &a, const TileGeo &g, float4 G,
+                                              float4 Lt, float4 &e) {
+    float dmin, dmax, lmin, lmax;
+    box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
+    box_bounds(a, g, Lt.x, Lt.y, Lt.z, lmin, lmax);
+    const float bmin = __fmaf_rn(a.sb, dmin, G.w) + __fmaf_rn(a.sa, lmin, Lt.w);
+    int32_t lo = (int32_t)floorf(bmin - kMargin);
+    const int32_t al = (int32_t)a.align;
+    lo -= ((lo % al) + al) % al;
+    e.x = __fmul_rn(G.x - __fmul_rn(g.ctr[0], a.h[0]), a.sb);
+    e.y = __fmul_rn(G.y - __fmul_rn(g.ctr[1], a.h[1]), a.sb);
+    e.z = __fmul_rn(G.z - __fmul_rn(g.ctr[2], a.h[2]), a.sb);
+    e.w = G.w - (float)lo;
+    return lo;
+}
+
+// Laser leg of voxel (ix, iy, iz) for laser entry Lt = (frame position, lw/dT - t0/dT).
+__device__ __forceinline__ float laser_leg(const FastArgs &a, uint32_t ix, uint32_t iy,
+                                           uint32_t iz, float4 Lt) {
+    const float dx = __fmaf_rn((float)ix, a.h[0], -Lt.x);
+    const float dy = __fmaf_rn((float)iy, a.h[1], -Lt.y);
+    const float dz = __fmaf_rn((float)iz, a.h[2], -Lt.z);
+    const float d = sqrtf(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))));
+    return __fmaf_rn(a.sa, d, Lt.w);
+}
+
+__device__ __forceinline__ float rel_coord(const FastArgs &a, const TileGeo &g, int k,
+                                           uint32_t idx) {
+    return __fmul_rn((float)idx - g.ctr[k], a.hs[k]);
+}
+
+// D = dx^2 + dy^2 + eps for one row, shared by the thread's K voxels.
+__device__ __forceinline__ float row_dxy(float vx, float vy, float4 e) {
+    const float dx = vx - e.x, dy = vy - e.y;
+    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, kQEps));
+}
+
+// Index into the row's window (as the float bits of x + 1.5*2^23).
+__device__ __forceinline__ uint32_t window_bits(float vz, float D, float A, float4 e) {
+    const float dz = vz - e.z;
+    const float q = __fmaf_rn(dz, dz, D);
+    const float r = rsqrt_approx(q);
+    const float x = __fmaf_rn(q, r, A);
+    const float y = __fadd_rn(x, e.w);
+    return __float_as_uint(__fadd_rn(y, kMagic));
+}
+
+template <typename HT>
+__device__ __forceinline__ void store_out(void *out, uint64_t i, const Acc<HT> &acc,
+                                          float scale);
+template <>
+__device__ __forceinline__ void store_out<float>(void *out, uint64_t i, const Acc<float> &acc,
+                                                 float scale) {
+    ((float *)out)[i] = acc.v * scale;
+}
+template <>
+__device__ __forceinline__ void store_out<__half>(void *out, uint64_t i,
+                                                  const Acc<__half> &acc, float scale) {
+    ((float *)out)[i] = acc.v * scale;
+}
+template <>
+__device__ __forceinline__ void store_out<__nv_bfloat16>(void *out, uint64_t i,
+                                                         const Acc<__nv_bfloat16> &acc,
+                                                         float scale) {
+    ((float *)out)[i] = acc.v * scale;
+}
+template <>
+__device__ __forceinline__ void store_out<float2>(void *out, uint64_t i, const Acc<float2> &acc,
+                                                  float scale) {
+    ((float2 *)out)[i] = make_float2(acc.v.x * scale, acc.v.y * scale);
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
+    const float y = x - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+template <typename HT, int K, bool KAHAN, bool CHECKED>
+__global__ void __launch_bounds__(288, 1)
+    bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
+                   const float4 *__restrict__ lasers, void *__restrict__ out,
+                   unsigned long long *__restrict__ diag, const FastArgs a) {
+    using AccT = Acc<HT>;
+    using Elem = typename AccT::Elem;
+    constexpr uint32_t esz = AccT::kBytes;
+
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[8];
+    __shared__ __align__(8) uint64_t empty_bar[8];
+    __shared__ int abort_flag;
+
+    // 128-byte aligned stage area
+    const uint32_t raw_addr = smem_addr(smem_raw);
+    const uint32_t pad = (128u - (raw_addr & 127u)) & 127u;
+    unsigned char *stage_base = smem_raw + pad;
+
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t n_cons = a.warp[0] * a.warp[1] * a.warp[2];
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    const uint32_t tile = (uint32_t)(blockIdx.x % ntiles);
+    const uint32_t split = (uint32_t)(blockIdx.x / ntiles);
+    const uint64_t items = a.L * a.nchunks;
+    const uint64_t i0 = items * split / a.splits, i1 = items * (split + 1) / a.splits;
+
+    TileGeo g;
+    tile_of_block(a, tile, g);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < a.stages; s++) {
+            mbar_init(smem_addr(&full_bar[s]), 1);
+            mbar_init(smem_addr(&empty_bar[s]), n_cons);
+        }
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        // ---------------- producer ----------------
+        uint64_t issued = 0;
+        for (uint64_t it = i0; it < i1; it++) {
+            const uint64_t i = it - i0;
+            const uint32_t stage = (uint32_t)(i % a.stages);
+            const uint32_t round = (uint32_t)(i / a.stages);
+            if (round > 0) {
+                // Every lane observes the consumers' release before its TMA overwrites
+                // the stage.
+                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (round - 1) & 1, a.spin_limit);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    if (lane == 0) {
+                        atomicAdd(&diag[0], 1ull);
+                        *(volatile int *)&abort_flag = 1;
+                    }
+                    break;
+                }
+            }
+            if (*(volatile int *)&abort_flag) break;
+            const uint64_t l = it / a.nchunks;
+            const uint64_t s0 = (it % a.nchunks) * a.chunk;
+            const uint32_t nrows = (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
+            unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
+            float4 *table = reinterpret_cast<float4 *>(st);
+            const uint32_t data = smem_addr(st + kTableBytes);
+            const uint32_t fb = smem_addr(&full_bar[stage]);
+            int32_t lo = 0;
+            if (lane < nrows) {
+                const float4 G = spads[s0 + lane];
+                const float4 Lt = lasers[l];
+                float4 e;
+                lo = row_record(a, g, G, Lt, e);
+                table[lane] = e;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
+            __syncwarp();
+            if (lane < nrows) {
+                const int32_t row = (int32_t)(l * a.S + s0 + lane);
+                const uint32_t dst = data + lane * a.row_bytes;
+                for (uint32_t b = 0; b < a.nbox; b++)
+                    tma_load_2d(dst + b * a.BW * esz, &tmap, lo + (int32_t)(b * a.BW), row, fb);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(fb);
+            issued = i + 1;
+        }
+        // Drain: every stage this CTA filled must have landed before the CTA may exit.
+        if (lane == 0) {
+            const uint64_t first = issued > a.stages ? issued - a.stages : 0;
+            for (uint64_t i = first; i < issued; i++) {
+                const uint32_t stage = (uint32_t)(i % a.stages);
+                if (!mbar_wait(smem_addr(&full_bar[stage]), (uint32_t)(i / a.stages) & 1,
+                               a.spin_limit))
+                    atomicAdd(&diag[0], 1ull);
+            }
+        }
+        return;
+    }
+
+    // ---------------- consumers ----------------
+    const uint32_t cw = warp - 1;
+    const uint32_t lxi = lane % a.lane[0], lyi = (lane / a.lane[0]) % a.lane[1];
+    const uint32_t lzi = lane / (a.lane[0] * a.lane[1]);
+    const uint32_t wxi = cw % a.warp[0], wyi = (cw / a.warp[0]) % a.warp[1];
+    const uint32_t wzi = cw / (a.warp[0] * a.warp[1]);
+    const uint32_t ix = g.org[0] + wxi * a.lane[0] + lxi;
+    const uint32_t iy = g.org[1] + wyi * a.lane[1] + lyi;
+    const uint32_t iz0 = g.org[2] + wzi * a.lane[2] * K + lzi;
+    const float vx = rel_coord(a, g, 0, ix), vy = rel_coord(a, g, 1, iy);
+    float vz[K], A[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) vz[k] = rel_coord(a, g, 2, iz0 + k * a.lane[2]);
+
+    AccT acc[K];
+    float comp[K][2];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        acc[k].zero();
+        comp[k][0] = comp[k][1] = 0.0f;
+    }
+    uint64_t cur_l = ~0ull;
+    uint32_t violations = 0;
+
+    for (uint64_t it = i0; it < i1; it++) {
+        const uint64_t i = it - i0;
+        const uint32_t stage = (uint32_t)(i % a.stages);
+        const uint32_t round = (uint32_t)(i / a.stages);
+        const uint64_t l = it / a.nchunks;
+        if (l != cur_l) {
+            const float4 Lt = lasers[l];
+#pragma unroll
+            for (int k = 0; k < K; k++) A[k] = laser_leg(a, ix, iy, iz0 + k * a.lane[2], Lt);
+            cur_l = l;
+        }
+        // Every lane acquires the stage (TMA bytes and the producer's row records).
+        bool ok = mbar_wait(smem_addr(&full_bar[stage]), round & 1, a.spin_limit);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok || *(volatile int *)&abort_flag) {
+            if (lane == 0 && !ok) {
+                atomicAdd(&diag[0], 1ull);
+                *(volatile int *)&abort_flag = 1;
+            }
+            break;
+        }
+        const uint64_t s0 = (it % a.nchunks) * a.chunk;
+        const uint32_t nrows = (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
+        const unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
+        const float4 *table = reinterpret_cast<const float4 *>(st);
+        const Elem *data = reinterpret_cast<const Elem *>(st + kTableBytes);
+        const uint32_t row_elems = a.row_bytes / esz;
+
+        AccT part[K];
+        if (KAHAN) {
+#pragma unroll
+            for (int k = 0; k < K; k++) part[k].zero();
+        }
+        for (uint32_t j = 0; j < nrows; j++) {
+            const float4 e = table[j];
+            const float D = row_dxy(vx, vy, e);
+            const uint32_t rbase = j * row_elems - kMagicBits;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                uint32_t idx = window_bits(vz[k], D, A[k], e) + rbase;
+                if (CHECKED) {
+                    const uint32_t rel = idx - j * row_elems;
+                    if (rel >= a.W) {
+                        violations++;
+                        idx = j * row_elems + ((int32_t)rel < 0 ? 0u : a.W - 1);
+                    }
+                }
+                if (KAHAN)
+                    part[k].add(data, idx);
+                else
+                    acc[k].add(data, idx);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&empty_bar[stage]));
+        if (KAHAN) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                if constexpr (sizeof(acc[k].v) == 8) {
+                    float2 pv = *reinterpret_cast<float2 *>(&part[k].v);
+                    float2 &av = *reinterpret_cast<float2 *>(&acc[k].v);
+                    kahan_add(av.x, comp[k][0], pv.x);
+                    kahan_add(av.y, comp[k][1], pv.y);
+                } else {
+                    float &av = *reinterpret_cast<float *>(&acc[k].v);
+                    kahan_add(av, comp[k][0], *reinterpret_cast<float *>(&part[k].v));
+                }
+            }
+        }
+    }
+    if (CHECKED && violations) atomicAdd(&diag[1], (unsigned long long)violations);
+    if (KAHAN) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if constexpr (sizeof(acc[k].v) == 8) {
+                float2 &av = *reinterpret_cast<float2 *>(&acc[k].v);
+                av.x -= comp[k][0];
+                av.y -= comp[k][1];
+            } else {
+                float &av = *reinterpret_cast<float *>(&acc[k].v);
+                av -= comp[k][0];
+            }
+        }
+    }
+    if (ix >= a.n[0] || iy >= a.n[1]) return;
+    const float scale = a.splits > 1 ? 1.0f : a.out_scale;
+    const uint64_t part_off = a.splits > 1 ? (uint64_t)split * a.nvox : 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const uint32_t iz = iz0 + k * a.lane[2];
+        if (iz < a.n[2])
+            store_out<HT>(out, part_off + ((uint64_t)ix * a.n[1] + iy) * a.n[2] + iz, acc[k],
+                          scale);
+    }
+}
+
+// out[v] = scale * sum_s partial[s][v], in split order (optionally Kahan).
+template <bool COMPLEX, bool KAHAN>
+__global__ void reduce_splits_kernel(const float *__restrict__ partial, float *__restrict__ out,
+                                     uint64_t nvox, uint32_t splits, float scale) {
+    constexpr int C = COMPLEX ? 2 : 1;
+    const uint64_t n = nvox * C;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float s = 0.0f, c = 0.0f;
+        for (uint32_t k = 0; k < splits; k++) {
+            const float x = partial[(uint64_t)k * n + i];
+            if (KAHAN)
+                kahan_add(s, c, x);
+            else
+                s += x;
+        }
+        if (KAHAN) s -= c;
+        out[i] = s * scale;
+    }
+}
+
+// bins[i * P + p] with the fast kernel's arithmetic for voxel ids[i] and pair p.
+__global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
+                                    const float4 *__restrict__ lasers,
+                                    const int64_t *__restrict__ ids, int64_t n,
+                                    int32_t *__restrict__ bins, const FastArgs a) {
+    const uint64_t P = a.L * a.S;
+    const uint64_t total = (uint64_t)n * P;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < total;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = w / P, p = w % P;
+        const int64_t id = ids[i];
+        const uint32_t iz = (uint32_t)(id % a.n[2]);
+        const uint32_t iy = (uint32_t)((id / a.n[2]) % a.n[1]);
+        const uint32_t ix = (uint32_t)(id / ((int64_t)a.n[1] * a.n[2]));
+        const uint32_t tile = ((iy / a.tdim[1]) * a.tiles[0] + ix / a.tdim[0]) * a.tiles[2] +
+                              iz / a.tdim[2];
+        TileGeo g;
+        tile_of_block(a, tile, g);
+        const uint64_t l = p / a.S, s = p % a.S;
+        const float4 Lt = lasers[l];
+        float4 e;
+        const int32_t lo = row_record(a, g, spads[s], Lt, e);
+        const float A = laser_leg(a, ix, iy, iz, Lt);
+        const float vx = rel_coord(a, g, 0, ix), vy = rel_coord(a, g, 1, iy);
+        const float vz = rel_coord(a, g, 2, iz);
+        const float D = row_dxy(vx, vy, e);
+        const int32_t rel = (int32_t)(window_bits(vz, D, A, e) - kMagicBits);
+        const int32_t b = lo + rel;
+        bins[w] = (b >= 0 && b < (int32_t)a.T) ? b : -1;
+    }
+}
+
+// Failure-path probe: one warp waits (bounded) on an mbarrier that nothing arrives on,
+// through the same wait helper the pipeline uses, and records whether it gave up.
+__global__ void wait_timeout_probe_kernel(uint32_t limit, unsigned long long *out) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_addr(&bar), 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    bool ok = mbar_wait(smem_addr(&bar), 0, limit);
+    ok = __all_sync(0xffffffffu, ok);
+    if (threadIdx.x == 0) out[0] = ok ? 0ull : 1ull;
+}
+
+// ---- tensor-map encoder from the driver (no libcuda link needed) -----------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                   CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+uint32_t dtype_bytes(int dt) {
+    switch (dt) {
+        case BPGB_DTYPE_F32: return 4;
+        case BPGB_DTYPE_F16:
+        case BPGB_DTYPE_BF16: return 2;
+        case BPGB_DTYPE_C64: return 8;
+    }
+    return 0;
+}
+
+CUtensorMapDataType tma_type(int dt) {
+    switch (dt) {
+        case BPGB_DTYPE_F16: return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+        case BPGB_DTYPE_BF16: return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+        case BPGB_DTYPE_C64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+        default: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    }
+}
+
+// Tile presets: {lx, ly, lz, k, wx, wy, wz, chunk, stages}.
+const FastConfig kPresets[] = {
+    {8, 4, 1, 8, 2, 2, 2, 32, 4},  // 16 x 8 x 16 tile, 2048 voxels
+    {4, 4, 2, 8, 4, 2, 1, 32, 4},  // 16 x 8 x 16, z pairs per lane
+    {8, 4, 1, 8, 2, 1, 4, 32, 4},  // 16 x 4 x 32
+    {4, 8, 1, 8, 2, 2, 2, 32, 4},  // 8 x 16 x 16
+    {8, 4, 1, 8, 1, 2, 4, 16, 4},  // 8 x 8 x 32
+    {8, 4, 1, 8, 2, 2, 2, 16, 3},  // 16 x 8 x 16, shallower stages
+};
+
+}  // namespace
+
+FastConfig fast_preset(int index, int dtype) {
+    (void)dtype;
+    const int n = (int)(sizeof(kPresets) / sizeof(kPresets[0]));
+    if (index < 0 || index >= n) index = 0;
+    return kPresets[index];
+}
+
+int fast_preset_count() { return (int)(sizeof(kPresets) / sizeof(kPresets[0])); }
+
+struct FastPlan {
+    FastArgs a{};
+    int dtype = 0;
+    bool kahan = false, checked = false;
+    uint64_t P = 0;
+    uint32_t pitch = 0;
+    uint32_t threads = 0, smem = 0, grid = 0;
+    float4 *d_tables = nullptr;  // S spad entries then L laser entries
+    unsigned long long *d_diag = nullptr;
+    float *d_partial = nullptr;
+    uint64_t scratch = 0;
+    int geom = 0;
+};
+
+namespace {
+
+template <typename HT, int K>
+void *kernel_ptr(bool kahan, bool checked) {
+    if (kahan)
+        return checked ? (void *)bp_fast_kernel<HT, K, true, true>
+                       : (void *)bp_fast_kernel<HT, K, true, false>;
+    return checked ? (void *)bp_fast_kernel<HT, K, false, true>
+                   : (void *)bp_fast_kernel<HT, K, false, false>;
+}
+
+void *select_kernel(int dtype, bool kahan, bool checked) {
+    switch (dtype) {
+        case BPGB_DTYPE_F16: return kernel_ptr<__half, 8>(kahan, checked);
+        case BPGB_DTYPE_BF16: return kernel_ptr<__nv_bfloat16, 8>(kahan, checked);
+        case BPGB_DTYPE_C64: return kernel_ptr<float2, 8>(kahan, checked);
+        default: return kernel_ptr<float, 8>(kahan, checked);
+    }
+}
+
+}  // namespace
+
+int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
+                    uint64_t P, const Factorization &fz, const Volume &vol,
+                    const BinParams &bp, const bpgb_options &opt, int sm_count,
+                    std::string *why_not) {
+    (void)d_pairs;
+    *out = nullptr;
+    auto no = [&](const std::string &m) {
+        if (why_not) *why_not = m;
+        return BPGB_ERR_UNSUPPORTED;
+    };
+    if (fz.geom != GEOM_SINGLE_LASER && fz.geom != GEOM_EXHAUSTIVE && fz.geom != GEOM_CONFOCAL)
+        return no("pair list does not factor as lasers x SPADs or confocal");
+    double u[3][3], hd[3];
+    if (!volume_frame(vol, u, hd)) return no("voxel basis is not orthogonal");
+    if (!encode_fn()) return no("cuTensorMapEncodeTiled unavailable");
+    const int dt = opt.h_dtype;
+    const uint32_t esz = dtype_bytes(dt);
+    if (!esz) return no("unknown H dtype");
+    const uint32_t pitch = opt.h_pitch ? opt.h_pitch : bp.T;
+    if (pitch < bp.T) return no("h_pitch < T");
+    if (((uint64_t)pitch * esz) % 16) return no("H row pitch is not a multiple of 16 bytes");
+    if (P >= (1ull << 31) || bp.T >= (1u << 30)) return no("P or T too large for TMA coordinates");
+    if (!(bp.dT > 0.0f)) return no("deltaT must be positive");
+
+    const FastConfig cfg = fast_preset(opt.tile, dt);
+    FastArgs a{};
+    for (int k = 0; k < 3; k++) a.n[k] = vol.n[k];
+    a.lane[0] = cfg.lx;
+    a.lane[1] = cfg.ly;
+    a.lane[2] = cfg.lz;
+    a.warp[0] = cfg.wx;
+    a.warp[1] = cfg.wy;
+    a.warp[2] = cfg.wz;
+    if (cfg.k != 8 || cfg.lx * cfg.ly * cfg.lz != 32) return no("bad tile preset");
+    for (int k = 0; k < 3; k++) {
+        a.tdim[k] = cfg.tile(k);
+        a.tiles[k] = (vol.n[k] + a.tdim[k] - 1) / a.tdim[k];
+    }
+    const bool confocal = fz.geom == GEOM_CONFOCAL;
+    const double dT = bp.dT;
+    const double sb = (confocal ? 2.0 : 1.0) / dT, sa = confocal ? 0.0 : 1.0 / dT;
+    a.sb = (float)sb;
+    a.sa = (float)sa;
+    for (int k = 0; k < 3; k++) {
+        a.h[k] = (float)hd[k];
+        a.hs[k] = (float)(hd[k] * sb);
+    }
+    a.L = confocal ? 1 : fz.L;
+    a.S = fz.S;
+    a.T = bp.T;
+    a.out_scale = opt.h_scale != 0.0f ? opt.h_scale : 1.0f;
+    a.nvox = vol.count();
+    a.spin_limit = opt.spin_limit ? opt.spin_limit : (1u << 22);
+
+    // Window width: the spread of (laser leg + SPAD leg) over a tile is at most
+    // (sa + sb) * tile diagonal (triangle inequality), plus margins and alignment.
+    double diag2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+        const double e = (double)(a.tdim[k] - 1) * hd[k];
+        diag2 += e * e;
+    }
+    const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
+    a.align = 16 / esz;
+    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
+    const uint32_t bw_align = 128 / esz;
+    a.nbox = (w_need + 255) / 256;
+    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
+    if (a.BW > 256) return no("window box too wide");
+    a.W = a.BW * a.nbox;
+    a.row_bytes = a.W * esz;
+
+    // Stage sizing: keep all stages within ~200 KB of shared memory.
+    const uint32_t budget = 200 * 1024;
+    uint32_t chunk = std::min<uint64_t>(std::min<uint32_t>(cfg.chunk, kMaxChunk), fz.S);
+    uint32_t stages = std::min<uint32_t>(cfg.stages, 8);
+    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
+    while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
+    while (stages > 2 && stages * stage_bytes(chunk) > budget) stages--;
+    if (stages * stage_bytes(chunk) > budget)
+        return no("time window of one tile does not fit in shared memory (" +
+                  std::to_string(a.W) + " bins)");
+    a.chunk = chunk;
+    a.stages = stages;
+    a.stage_bytes = stage_bytes(chunk);
+    a.nchunks = (uint32_t)((fz.S + chunk - 1) / chunk);
+
+    auto *fp = new FastPlan();
+    fp->dtype = dt;
+    fp->kahan = opt.accum == BPGB_ACCUM_KAHAN;
+    fp->checked = opt.checked != 0;
+    fp->P = P;
+    fp->pitch = pitch;
+    fp->geom = fz.geom;
+    fp->threads = 32 * (1 + cfg.wx * cfg.wy * cfg.wz);
+    fp->smem = a.stages * a.stage_bytes + 128;
+
+    void *kern = select_kernel(dt, fp->kahan, fp->checked);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)fp->smem);
+    if (e != cudaSuccess) {
+        delete fp;
+        return cuda_error(e, "cudaFuncSetAttribute(fast kernel)");
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)fp->threads, fp->smem);
+    if (e != cudaSuccess || occ < 1) {
+        delete fp;
+        return e != cudaSuccess ? cuda_error(e, "occupancy query")
+                                : no("fast kernel does not fit on an SM");
+    }
+
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    const uint64_t items = a.L * a.nchunks;
+    uint64_t splits = opt.pair_splits > 0 ? (uint64_t)opt.pair_splits : 1;
+    if (opt.pair_splits <= 0) {
+        const uint64_t want = 2ull * sm_count * occ;  // two waves of resident CTAs
+        if (ntiles < want) splits = (want + ntiles - 1) / ntiles;
+    }
+    splits = std::max<uint64_t>(1, std::min<uint64_t>(splits, items));
+    if (ntiles * splits >= (1ull << 31)) {
+        delete fp;
+        return no("grid too large");
+    }
+    a.splits = (uint32_t)splits;
+    fp->grid = (uint32_t)(ntiles * splits);
+    fp->a = a;
+
+    // Device tables: SPAD entries (frame position relative to zero, row constant) and
+    // laser entries (frame position, lw/dT - t0/dT), built in double on the host.
+    std::vector<float4> tab(fz.S + a.L);
+    auto frame = [&](const float *pt, double o[3]) {
+        double d[3];
+        for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
+        for (int r = 0; r < 3; r++) o[r] = u[r][0] * d[0] + u[r][1] * d[1] + u[r][2] * d[2];
+    };
+    for (uint64_t s = 0; s < fz.S; s++) {
+        const bpgb_pair &pr = h_pairs[s];
+        double f[3];
+        frame(pr.camera_point, f);
+        const double cs = confocal ? ((double)pr.camera_wall + (double)pr.laser_wall) / dT
+                                   : (double)pr.camera_wall / dT;
+        tab[s] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)cs);
+    }
+    for (uint64_t l = 0; l < a.L; l++) {
+        double f[3] = {0.0, 0.0, 0.0};
+        double c = -(double)bp.t0 / dT;
+        if (!confocal) {
+            const bpgb_pair &pr = h_pairs[l * fz.S];
+            frame(pr.laser_point, f);
+            c += (double)pr.laser_wall / dT;
+        }
+        tab[fz.S + l] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)c);
+    }
+    const size_t tab_bytes = tab.size() * sizeof(float4);
+    const size_t part_bytes =
+        splits > 1 ? (size_t)splits * a.nvox * (dt == BPGB_DTYPE_C64 ? 8 : 4) : 0;
+    e = cudaMalloc(&fp->d_tables, tab_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess && part_bytes) e = cudaMalloc(&fp->d_partial, part_bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(fp->d_tables, tab.data(), tab_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(fp->d_diag, 0, 2 * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        fast_plan_free(fp);
+        return e == cudaErrorMemoryAllocation ? set_error(BPGB_ERR_OUT_OF_MEMORY, "fast plan scratch")
+                                              : cuda_error(e, "fast plan tables");
+    }
+    fp->scratch = tab_bytes + part_bytes + 16;
+    *out = fp;
+    return BPGB_OK;
+}
+
+int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t stream) {
+    const FastArgs &a = fp->a;
+    const uint32_t esz = dtype_bytes(fp->dtype);
+    if (((uintptr_t)d_H) % 16) return set_error(BPGB_ERR_INVALID_ARGUMENT, "H must be 16-byte aligned");
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {a.T, fp->P};
+    const cuuint64_t strides[1] = {(cuuint64_t)fp->pitch * esz};
+    const cuuint32_t box[2] = {a.BW, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&map, tma_type(fp->dtype), 2, const_cast<void *>(d_H), dims, strides,
+                             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
+    const float4 *spads = fp->d_tables;
+    const float4 *lasers = fp->d_tables + a.S;
+    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked);
+    void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
+                    (void *)&fp->d_diag, (void *)&fp->a};
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
+    count_launches(1);
+    if (a.splits > 1) {
+        const bool cplx = fp->dtype == BPGB_DTYPE_C64;
+        const uint64_t n = a.nvox * (cplx ? 2 : 1);
+        const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8);
+        if (cplx) {
+            if (fp->kahan)
+                reduce_splits_kernel<true, true><<<blocks, 256, 0, stream>>>(
+                    fp->d_partial, (float *)d_out, a.nvox, a.splits, a.out_scale);
+            else
+                reduce_splits_kernel<true, false><<<blocks, 256, 0, stream>>>(
+                    fp->d_partial, (float *)d_out, a.nvox, a.splits, a.out_scale);
+        } else {
+            if (fp->kahan)
+                reduce_splits_kernel<false, true><<<blocks, 256, 0, stream>>>(
+                    fp->d_partial, (float *)d_out, a.nvox, a.splits, a.out_scale);
+            else
+                reduce_splits_kernel<false, false><<<blocks, 256, 0, stream>>>(
+                    fp->d_partial, (float *)d_out, a.nvox, a.splits, a.out_scale);
+        }
+        count_launches(1);
+        BPGB_CUDA_TRY(cudaGetLastError());
+    }
+    return BPGB_OK;
+}
+
+int fast_plan_dump_bins(FastPlan *fp, const int64_t *d_ids, int64_t n, int32_t *d_bins,
+                        cudaStream_t stream) {
+    if (n <= 0) return BPGB_OK;
+    const uint64_t total = (uint64_t)n * fp->P;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((total + 255) / 256, 152ull * 16);
+    bp_fast_bins_kernel<<<blocks, 256, 0, stream>>>(fp->d_tables, fp->d_tables + fp->a.S, d_ids,
+                                                     n, d_bins, fp->a);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info) {
+    const FastArgs &a = fp->a;
+    info->algo = BPGB_ALGO_FAST;
+    info->geometry = fp->geom;
+    info->num_lasers = a.L;
+    info->num_spads = a.S;
+    for (int k = 0; k < 3; k++) info->tile[k] = a.tdim[k];
+    info->window = a.W;
+    info->chunk = a.chunk;
+    info->stages = a.stages;
+    info->pair_splits = a.splits;
+    info->grid = fp->grid;
+    info->threads = fp->threads;
+    info->smem_bytes = fp->smem;
+    info->scratch_bytes = fp->scratch;
+}
+
+int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts) {
+    unsigned long long h[2] = {0, 0};
+    BPGB_CUDA_TRY(cudaMemcpy(h, fp->d_diag, sizeof(h), cudaMemcpyDeviceToHost));
+    BPGB_CUDA_TRY(cudaMemset(fp->d_diag, 0, sizeof(h)));
+    if (violations) *violations = h[1];
+    if (timeouts) *timeouts = h[0];
+    return BPGB_OK;
+}
+
+int wait_timeout_probe(uint32_t limit, int *timed_out) {
+    unsigned long long *d = nullptr;
+    BPGB_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
+    wait_timeout_probe_kernel<<<1, 32>>>(limit, d);
+    count_launches(1);
+    unsigned long long h = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_error(e, "wait timeout probe");
+    *timed_out = h ? 1 : 0;
+    return BPGB_OK;
+}
+
+void fast_plan_free(FastPlan *fp) {
+    if (!fp) return;
+    if (fp->d_tables) cudaFree(fp->d_tables);
+    if (fp->d_diag) cudaFree(fp->d_diag);
+    if (fp->d_partial) cudaFree(fp->d_partial);
+    delete fp;
+}
+
+}  // namespace bpgb

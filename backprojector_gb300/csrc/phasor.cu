@@ -1,0 +1,155 @@
+// Phasor-field pulse convolution (bp::phasor_pulse, backproject.hpp:430-479) on the GPU.
+//
+// out[r, t] = sum_{k=0}^{K-1} H[r, t + k - K/2] * (cos_k, sin_k) over read indices in
+// (0, T) (index 0 is excluded, :468).  The sum runs in tap order with a separate FP32
+// multiply and add per tap, as the reference's loop does, so the result matches a CPU
+// evaluation of that loop bit for bit.  Each CTA stages one row segment plus its halo
+// in shared memory (zeros outside (0, T), which reproduces the index test), and each
+// thread produces 8 outputs strided by the block size (conflict-free shared reads).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "bpgb_internal.h"
+
+namespace bpgb {
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kPerThread = 8;
+constexpr int kSeg = kThreads * kPerThread;
+
+__global__ void __launch_bounds__(kThreads)
+    phasor_pulse_kernel(const float *__restrict__ H, uint32_t T, uint32_t in_pitch,
+                        const float2 *__restrict__ taps, int K, float2 *__restrict__ out,
+                        uint32_t out_pitch, uint32_t nseg) {
+    extern __shared__ float sm[];
+    float *seg = sm;                                         // kSeg + K entries
+    float2 *tp = reinterpret_cast<float2 *>(sm + ((kSeg + K + 1) & ~1));
+    const uint64_t r = blockIdx.x / nseg;
+    const uint32_t sg = blockIdx.x % nseg;
+    const int64_t t_begin = (int64_t)sg * kSeg;
+    const int half = K / 2;
+    const float *row = H + r * in_pitch;
+    for (int i = threadIdx.x; i < kSeg + K; i += kThreads) {
+        const int64_t ri = t_begin - half + i;
+        seg[i] = (ri > 0 && ri < (int64_t)T) ? row[ri] : 0.0f;
+    }
+    for (int k = threadIdx.x; k < K; k += kThreads) tp[k] = taps[k];
+    __syncthreads();
+    float re[kPerThread], im[kPerThread];
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++) re[j] = im[j] = 0.0f;
+    for (int k = 0; k < K; k++) {
+        const float2 c = tp[k];
+#pragma unroll
+        for (int j = 0; j < kPerThread; j++) {
+            const float x = seg[threadIdx.x + j * kThreads + k];
+            re[j] = __fadd_rn(re[j], __fmul_rn(x, c.x));
+            im[j] = __fadd_rn(im[j], __fmul_rn(x, c.y));
+        }
+    }
+    float2 *orow = out + r * out_pitch;
+#pragma unroll
+    for (int j = 0; j < kPerThread; j++) {
+        const int64_t t = t_begin + threadIdx.x + j * kThreads;
+        if (t < (int64_t)T) orow[t] = make_float2(re[j], im[j]);
+    }
+}
+
+}  // namespace
+
+int launch_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch,
+                        const float *h_taps, int K, float *d_out, uint32_t out_pitch,
+                        cudaStream_t stream) {
+    if (rows == 0 || T == 0) return BPGB_OK;
+    if (K <= 0) {
+        for (uint64_t r = 0; r < rows; r++)
+            BPGB_CUDA_TRY(cudaMemsetAsync(d_out + 2 * r * out_pitch, 0, (size_t)T * 8, stream));
+        return BPGB_OK;
+    }
+    // taps as interleaved (cos, sin) pairs on the device (stream-ordered scratch)
+    std::vector<float2> tp(K);
+    for (int k = 0; k < K; k++) tp[k] = make_float2(h_taps[k], h_taps[K + k]);
+    float2 *d_taps = nullptr;
+    BPGB_CUDA_TRY(cudaMallocAsync(&d_taps, K * sizeof(float2), stream));
+    cudaError_t e = cudaMemcpyAsync(d_taps, tp.data(), K * sizeof(float2),
+                                    cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // tp is a host temporary
+    if (e != cudaSuccess) {
+        cudaFreeAsync(d_taps, stream);
+        return cuda_error(e, "phasor taps upload");
+    }
+    const uint32_t nseg = (T + kSeg - 1) / kSeg;
+    const size_t smem = (size_t)(((kSeg + K + 1) & ~1) + 2 * K) * sizeof(float);
+    if (smem > 200 * 1024) {
+        cudaFreeAsync(d_taps, stream);
+        return set_error(BPGB_ERR_UNSUPPORTED, "phasor pulse too long for shared memory");
+    }
+    e = cudaFuncSetAttribute(phasor_pulse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(d_taps, stream);
+        return cuda_error(e, "phasor smem attribute");
+    }
+    const uint64_t blocks = rows * nseg;
+    if (blocks >= (1ull << 31)) {
+        cudaFreeAsync(d_taps, stream);
+        return set_error(BPGB_ERR_UNSUPPORTED, "too many rows for one launch");
+    }
+    phasor_pulse_kernel<<<(unsigned)blocks, kThreads, smem, stream>>>(
+        d_H, T, in_pitch, d_taps, K, reinterpret_cast<float2 *>(d_out), out_pitch, nseg);
+    count_launches(1);
+    e = cudaGetLastError();
+    cudaFreeAsync(d_taps, stream);
+    if (e != cudaSuccess) return cuda_error(e, "phasor pulse launch");
+    return BPGB_OK;
+}
+
+}  // namespace bpgb
+
+extern "C" {
+
+int bpgb_phasor_taps(float wavelength, float deltaT, uint32_t times, float *taps, int cap) {
+    // Reference construction (backproject.hpp:433-451): K = int(times*wl/dT),
+    // C = int(wl/dT), sigma = times*wl/6; t_k = dT*(k - K/2.0) for k = 1..K; Gaussian
+    // exp(-t^2 / (2 sigma^2)) in double with 2*sigma*sigma an FP32 product; phase
+    // 2*pi*(k/C); cos/sin rounded to FP32, times the Gaussian in double, rounded to FP32.
+    const int K = (int)((float)times * wavelength / deltaT);
+    const int C = (int)(wavelength / deltaT);
+    if (K <= 0 || C <= 0 || !taps || cap < K) return K;
+    const float vsigma = ((float)times * wavelength) / 6.0f;
+    const double denom = (double)(2.0f * vsigma * vsigma);
+    for (int k = 0; k < K; k++) {
+        const double kk = (double)(k + 1);
+        const double t = (double)deltaT * (kk - K / 2.0);
+        const double g = std::exp(-t * t / denom);
+        const double prog = 2.0 * M_PI * (1.0 / C * kk);
+        const float s = (float)std::sin(prog);
+        const float c = (float)std::cos(prog);
+        taps[k] = (float)((double)c * g);
+        taps[K + k] = (float)((double)s * g);
+    }
+    return K;
+}
+
+int bpgb_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch,
+                      float wavelength, float deltaT, uint32_t times, float *d_out,
+                      uint32_t out_pitch, void *stream) {
+    bpgb::clear_error();
+    if ((rows && (!d_H || !d_out)) || in_pitch < T || out_pitch < T)
+        return bpgb::set_error(BPGB_ERR_INVALID_ARGUMENT, "bad phasor pulse arguments");
+    if (!(deltaT > 0.0f) || !(wavelength > 0.0f))
+        return bpgb::set_error(BPGB_ERR_INVALID_ARGUMENT, "wavelength and deltaT must be > 0");
+    int st = bpgb::require_device();
+    if (st) return st;
+    const int K = bpgb_phasor_taps(wavelength, deltaT, times, nullptr, 0);
+    std::vector<float> taps(K > 0 ? 2 * (size_t)K : 1);
+    if (K > 0) bpgb_phasor_taps(wavelength, deltaT, times, taps.data(), K);
+    return bpgb::launch_phasor_pulse(d_H, rows, T, in_pitch, taps.data(), K, d_out, out_pitch,
+                                     (cudaStream_t)stream);
+}
+
+}  // extern "C"

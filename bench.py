@@ -1,0 +1,357 @@
+"""Benchmark: voxel-pair updates/s of the dense backprojection on one GB300.
+
+Workload (default): the learned-octree target capture at its dense form -- one laser,
+128 x 128 SPADs on a 2 x 2 m wall, T = 4096 bins (deltaT 1.5 mm), 256^3 voxels over a
+1.5 m cube; P = 16384 pairs, 2.75e11 voxel-pair updates per reconstruction.  One step =
+one full reconstruction of a seeded synthetic capture (see backprojector_gb300/synthetic.py).
+
+JSON line keys beyond the contract's: roofline (the FAST kernel against the GB300's
+reciprocal-square-root issue rate, one MUFU op per update), cpu_baseline (the
+reference's OpenMP CPU path restated in C, timed on a bounded voxel sample on the host
+cores), e2e (the drop-in host-buffer C ABI call, host<->device copies included),
+reference_gpu_kernel (the reference's own kernel built from its sources, one run).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "octree_256": "dense, 1 laser x 128x128 SPADs, T=4096, dT=1.5mm, 256^3 over a 1.5 m cube",
+    "precision_64": "dense, 1 laser x 64x64 SPADs, T=2048, dT=1mm, 64^3 over a 1 m cube",
+    "dense_exhaustive_16": "dense, 16x16 lasers x 16x16 SPADs, T=512, dT=3mm, 32^3 over 0.5 m",
+    "phasor_128": "phasor complex64, 1 laser x 128x128 SPADs, T=4096, dT=0.5mm, 128^3 over 1.5 m",
+}
+MUFU_PER_SM_PER_CLK = 16  # reciprocal square root throughput of one SM (Blackwell SFU)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i] == "Active"})
+        pw = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "power_w_max": max(pw) if pw else None, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def cpu_baseline(cap, sample_voxels: int, seed: int = 0):
+    """The reference's OpenMP CPU path (classic_backprojection, backproject.hpp:138-216,
+    restated in oracle/oracle.c) on a seeded voxel sample, all host threads."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(seed)
+    ids = rng.choice(cap.nvox, size=min(sample_voxels, cap.nvox), replace=False)
+    t = time.perf_counter()
+    oracle.classic(cap.H, cap.pairs, cap.voxels_per_side, cap.volume_position, cap.volume_size,
+                   cap.t0, cap.deltaT, voxels=ids)
+    dt = time.perf_counter() - t
+    return len(ids) * cap.P / dt, dt, len(ids), oracle.num_threads()
+
+
+def run_reference_arm(args):
+    """--impl reference: the reference's CPU implementation of the path on host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from backprojector_gb300 import synthetic
+
+    cap = synthetic.make_capture(args.workload, seed=args.seed)
+    for _ in range(args.warmup):
+        cpu_baseline(cap, args.ref_sample, seed=1)
+    rates, secs = [], []
+    cores = None
+    for k in range(args.steps):
+        r, dt, n, cores = cpu_baseline(cap, args.ref_sample, seed=100 + k)
+        rates.append(r)
+        secs.append(dt)
+    value = float(np.sum([args.ref_sample * cap.P for _ in rates]) / np.sum(secs))
+    line = {
+        "impl": "reference", "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(secs) * 1e3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload]}",
+                   "sample": f"{args.ref_sample} seeded random voxels x all {cap.P} pairs per step"},
+        "cpu_baseline": {"value": value, "unit": "updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.ref_sample} voxels x {cap.P} pairs per step; "
+                                   "classic_backprojection restated in C (OpenMP)"},
+        "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    from backprojector_gb300 import capi, synthetic
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    cap = synthetic.make_capture(args.workload, seed=args.seed + rank)
+    phasor = args.workload == "phasor_128"
+    N = tuple(int(v) for v in cap.voxels_per_side)
+    stream = torch.cuda.Stream(device=dev)
+    opt = dict(algo=capi.ALGO_FAST if args.algo == "fast" else capi.ALGO_EXACT)
+    if args.dtype == "f16":
+        opt["h_dtype"] = capi.DTYPE_F16
+    if args.kahan:
+        opt["accum"] = capi.ACCUM_KAHAN
+    if args.tile is not None:
+        opt["tile"] = args.tile
+    if phasor:
+        Hdev = torch.from_numpy(cap.H).to(dev)
+        Hc = torch.empty(cap.H.shape, dtype=torch.complex64, device=dev)
+        capi.phasor_pulse_device(Hdev, cap.P, cap.T, cap.T, cap.wavelength, cap.deltaT, Hc, cap.T)
+        torch.cuda.synchronize()
+        dH = Hc
+        opt["h_dtype"] = capi.DTYPE_C64
+        dV = torch.empty(N, dtype=torch.complex64, device=dev)
+    else:
+        dH = torch.from_numpy(cap.H).to(dev)
+        scale = 1.0
+        if args.dtype == "f16":
+            scale = float(cap.H.max()) / 1024.0 or 1.0
+            dH = (dH / scale).half()
+            opt["h_scale"] = scale
+        dV = torch.empty(N, dtype=torch.float32, device=dev)
+    # Gate: the bounds-checked kernel variant must see every bin inside its staged window
+    # before the unchecked variant runs.
+    with capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, checked=1,
+                   **opt) as gate:
+        gate.execute(dH, dV)
+        if gate.check() != 0:
+            raise RuntimeError("window check failed: bins outside the staged windows")
+    plan = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, **opt)
+    info = plan.info()
+
+    def step():
+        plan.execute(dH, dV, stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+    plan.check()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = capi.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    launches = capi.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    plan.check()
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    updates = cap.updates
+    value = updates * ws / (ms * 1e-3)
+
+    # e2e: the drop-in C ABI call on pinned host buffers (copies inside the call)
+    e2e = None
+    if not phasor and args.dtype == "f32":
+        hH = torch.from_numpy(cap.H).pin_memory()
+        hV = torch.empty(N, dtype=torch.float32).pin_memory()
+        L = capi.lib()
+        n = np.asarray(N, np.uint32)
+        o = capi.options(**{k: v for k, v in opt.items() if k != "h_scale"})
+        import ctypes as C
+
+        def e2e_call():
+            st = L.bpgb_backproject_host(C.c_void_p(hH.data_ptr()), cap.P * cap.T, cap.T,
+                                         capi.vptr(cap.pairs), cap.P, C.c_void_p(hV.data_ptr()),
+                                         capi.u32ptr(n), capi.fptr(cap.zero), capi.fptr(cap.inc),
+                                         cap.t0, cap.deltaT, C.byref(o))
+            capi.check(st, "bpgb_backproject_host")
+
+        for _ in range(max(1, args.warmup // 2)):
+            e2e_call()
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_call()
+        e2e_s = (time.perf_counter() - t) / args.steps
+        e2e = {"value": updates * ws / e2e_s, "unit": "updates/s",
+               "h2d_bytes_per_step": int(cap.H.nbytes), "d2h_bytes_per_step": int(cap.nvox * 4),
+               "ms_per_step": e2e_s * 1e3,
+               "path": "bpgb_backproject_host (plan + H2D + kernel + D2H, synchronous)"}
+
+    peaks = measured_peaks()
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak_updates = sms * MUFU_PER_SM_PER_CLK * sm_mhz * 1e6
+    achieved = updates / (ms * 1e-3)
+    esz = {"f32": 4, "f16": 2}[args.dtype] if not phasor else 8
+    algo_bytes = cap.P * cap.T * esz + cap.nvox * (8 if phasor else 4)
+    roofline = {
+        "bound": "sfu", "kernel": "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel",
+        "achieved": achieved, "peak": peak_updates, "unit": "voxel-pair updates/s",
+        "frac": achieved / peak_updates,
+        "peak_basis": f"{sms} SMs x {MUFU_PER_SM_PER_CLK} rsqrt/clk x {sm_mhz:.0f} MHz "
+                      "(median SM clock sampled during the timed region); one rsqrt per update",
+        "traffic": None,
+        "algorithmic_bytes": algo_bytes,
+        "hbm_achieved_gbs": algo_bytes / (ms * 1e-3) / 1e9,
+        "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        "hbm_frac": algo_bytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+    }
+    tr = ROOT / "profiles" / f"traffic_{args.workload}.json"
+    if tr.exists():
+        try:
+            roofline["traffic"] = json.loads(tr.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            pass
+
+    line = {
+        "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"f32": "f32", "f16": "f16 storage, f32 accumulate"}[args.dtype] if not phasor
+        else "complex64",
+        "data": "synthetic (seeded scene rendered per pair; no dataset available)",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload]}", "P": cap.P,
+                   "T": cap.T, "voxels": list(N), "updates_per_step": updates,
+                   "l2": f"inputs larger than L2 (H = {cap.H.nbytes / 1e6:.0f} MB > 129 MB)",
+                   "plan": info, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        r, dt, nvs, cores = cpu_baseline(cap, args.cpu_sample)
+        line["cpu_baseline"] = {"value": r, "unit": "updates/s", "cores": cores, "kind": "port",
+                                "sample": f"{nvs} seeded random voxels x all {cap.P} pairs "
+                                          f"({dt:.1f} s); reference classic_backprojection "
+                                          "restated in C with OpenMP"}
+    if rank == 0 and not args.no_ref_gpu and not phasor:
+        line["reference_gpu_kernel"] = reference_gpu(cap)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_gpu(cap):
+    """The reference's own kernel (built from its sources) on this GPU: one run."""
+    try:
+        from oracle import oracle
+
+        if not oracle.REF_LIB.exists():
+            return {"unavailable": "reference cubin/loader not built"}
+        vol, block, ms = oracle.reference_gpu(cap.H, cap.pairs, cap.voxels_per_side, cap.zero,
+                                              cap.inc, cap.t0, cap.deltaT)
+        return {"value": cap.updates / (ms * 1e-3), "unit": "updates/s", "ms": ms,
+                "block": block, "note": "launch loop only (its own 16^3-grid relaunch policy)"}
+    except Exception as e:  # reported, never fatal
+        return {"unavailable": str(e)[:200]}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="octree_256")
+    ap.add_argument("--algo", choices=["fast", "exact"], default="fast")
+    ap.add_argument("--dtype", choices=["f32", "f16"], default="f32")
+    ap.add_argument("--kahan", action="store_true")
+    ap.add_argument("--tile", type=int, default=None)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--ref-sample", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

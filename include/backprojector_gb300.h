@@ -1,0 +1,230 @@
+/*
+ * backprojector_gb300 -- C ABI of the GB300 (sm_103a) NLOS backprojection engine.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, returns an int
+ * status (0 = ok, negative = error; see bpgb_status) and never exits the process.
+ * bpgb_last_error() returns a message for the last failure on the calling thread.
+ *
+ * Reference interfaces replaced (mjgalindo/backprojector):
+ *   bpgb_backproject_f32  <- call_cuda_backprojection          backproject_cuda.hpp:19-28
+ *                            (implementation backproject_cuda.cu:370-500)
+ *   bpgb_backproject_c64  <- call_cuda_complex_backprojection  backproject_cuda.hpp:41-49
+ *                            (implementation backproject_cuda.cu:671-801)
+ *   bpgb_pair             <- struct CameraLaserPair            backproject_cuda.hpp:9-13
+ *   bpgb_plan_*           <- the launch policy of the same launchers, split into a
+ *                            reusable plan (geometry analysed once) and an asynchronous,
+ *                            stream-ordered execute on device buffers.
+ *   bpgb_phasor_pulse     <- bp::phasor_pulse                  backproject.hpp:430-479
+ *   bpgb_precompute_pairs <- bp::precompute_distances          backproject.hpp:356-418
+ *   bpgb_volume_basis     <- volume basis / voxel_inc          backproject.hpp:820-839
+ *   bpgb_time_limits      <- bp::get_time_limits               backproject.hpp:617-674
+ *   bpgb_backproject_capture / bpgb_phasor_capture
+ *                         <- bp::backproject / bp::phasor_reconstruction
+ *                            backproject.hpp:762-909 / 932-1039 (GPU, Naive access)
+ *
+ * Threading: every call is safe from several host threads on distinct plans and
+ * buffers.  A plan must not be executed concurrently with itself.
+ */
+#ifndef BACKPROJECTOR_GB300_H
+#define BACKPROJECTOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BPGB_ABI_VERSION 1
+
+/* One (laser point, SPAD point) pair with its origin-to-wall legs.  Byte layout is the
+ * reference's CameraLaserPair: camera point first, 32 bytes. */
+typedef struct bpgb_pair {
+    float camera_point[3];
+    float laser_point[3];
+    float camera_wall;
+    float laser_wall;
+} bpgb_pair;
+
+typedef enum bpgb_status {
+    BPGB_OK = 0,
+    BPGB_ERR_INVALID_ARGUMENT = -1, /* shapes, NaN geometry, null pointers */
+    BPGB_ERR_CUDA = -2,             /* a CUDA runtime call or launch failed */
+    BPGB_ERR_OUT_OF_MEMORY = -3,    /* device allocation failed */
+    BPGB_ERR_TIMEOUT = -4,          /* a bounded device-side wait gave up */
+    BPGB_ERR_UNSUPPORTED = -5,      /* valid request the selected algorithm cannot serve */
+    BPGB_ERR_NO_DEVICE = -6,        /* no CUDA device of compute capability 10.3 */
+    BPGB_ERR_WINDOW = -7            /* checked mode saw a bin outside its staged window */
+} bpgb_status;
+
+/* Storage type of the transient rows H[pair, time]. */
+typedef enum bpgb_dtype {
+    BPGB_DTYPE_F32 = 0,
+    BPGB_DTYPE_F16 = 1,
+    BPGB_DTYPE_BF16 = 2,
+    BPGB_DTYPE_C64 = 3 /* interleaved (re, im) float pairs */
+} bpgb_dtype;
+
+typedef enum bpgb_algo {
+    BPGB_ALGO_AUTO = 0,  /* FAST when the geometry allows it, else EXACT */
+    BPGB_ALGO_EXACT = 1, /* the reference's FP32 expression: bin indices bit-identical */
+    BPGB_ALGO_FAST = 2   /* factored legs, TMA-staged windows, sqrt.approx */
+} bpgb_algo;
+
+typedef enum bpgb_accum {
+    BPGB_ACCUM_F32 = 0,  /* plain FP32 running sums */
+    BPGB_ACCUM_KAHAN = 1 /* FP32 chunk sums folded with Kahan compensation */
+} bpgb_accum;
+
+typedef struct bpgb_options {
+    int32_t algo;        /* bpgb_algo */
+    int32_t h_dtype;     /* bpgb_dtype */
+    int32_t accum;       /* bpgb_accum */
+    uint32_t h_pitch;    /* elements between consecutive H rows (0 = T) */
+    float h_scale;       /* result multiplier (FP16/BF16 per-capture scale; 0 = 1) */
+    int32_t tile;        /* tile preset index (-1 = tuned default) */
+    int32_t pair_splits; /* CTAs sharing one voxel tile over disjoint pair ranges (0 = auto) */
+    int32_t checked;     /* 1 = clamp and count out-of-window bins (tests) */
+    uint32_t spin_limit; /* bounded mbarrier waits: polls before giving up (0 = default) */
+    int32_t reserved[7];
+} bpgb_options;
+
+/* Read-only description of a plan, for tests, the bench and the autotuner. */
+typedef struct bpgb_plan_info {
+    int32_t algo;        /* algorithm selected (EXACT or FAST) */
+    int32_t geometry;    /* 0 generic, 1 single laser, 2 exhaustive (L x S), 3 confocal */
+    uint64_t num_lasers; /* L of the factorisation (P when generic) */
+    uint64_t num_spads;  /* S of the factorisation (1 when generic) */
+    uint32_t tile[3];    /* voxels per CTA tile along x, y, z */
+    uint32_t window;     /* staged time bins per pair and tile (FAST) */
+    uint32_t chunk;      /* pairs per pipeline stage (FAST) */
+    uint32_t stages;     /* pipeline depth (FAST) */
+    uint32_t pair_splits;
+    uint32_t grid;       /* CTAs per execute */
+    uint32_t threads;    /* threads per CTA */
+    uint32_t smem_bytes; /* dynamic shared memory per CTA */
+    uint64_t scratch_bytes; /* device scratch held by the plan */
+    uint64_t updates;    /* voxel x pair updates per execute */
+} bpgb_plan_info;
+
+typedef struct bpgb_plan_s *bpgb_plan;
+
+/* ---- library ----------------------------------------------------------- */
+int bpgb_abi_version(void);
+const char *bpgb_status_string(int status);
+const char *bpgb_last_error(void);
+void bpgb_options_default(bpgb_options *opt);
+/* Number of kernel launches this process made through the library so far. */
+uint64_t bpgb_launch_count(void);
+
+/* ---- drop-in host-buffer calls ------------------------------------------
+ * Same arguments and meaning as the reference: caller-owned HOST buffers,
+ * transient_size = P * T elements, the voxel volume [Nx, Ny, Nz] (x slowest) is
+ * OVERWRITTEN, the call is synchronous on the current device.  Unlike the reference,
+ * every pair is used (it skips the last P mod blockDim pairs) and every voxel is
+ * visited for any N (its voxel cursor skips voxels when N is not a multiple of 16).
+ * ALGO_AUTO, FP32 accumulation.  Replaces backproject_cuda.cu:370-500 / 671-801. */
+int bpgb_backproject_f32(const float *transient_chunk, uint64_t transient_size, uint32_t T,
+                         const bpgb_pair *scanned_pairs, uint64_t num_pairs,
+                         float *voxel_volume, const uint32_t *voxels_per_side,
+                         const float *volume_zero_pos, const float *voxel_inc, float t0,
+                         float deltaT);
+/* transient_chunk and voxel_volume hold interleaved complex64 (re, im). */
+int bpgb_backproject_c64(const float *transient_chunk, uint64_t transient_size, uint32_t T,
+                         const bpgb_pair *scanned_pairs, uint64_t num_pairs,
+                         float *voxel_volume, const uint32_t *voxels_per_side,
+                         const float *volume_zero_pos, const float *voxel_inc, float t0,
+                         float deltaT);
+/* As bpgb_backproject_f32/_c64 with explicit options (algo, accumulation). */
+int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, uint32_t T,
+                          const bpgb_pair *scanned_pairs, uint64_t num_pairs,
+                          void *voxel_volume, const uint32_t *voxels_per_side,
+                          const float *volume_zero_pos, const float *voxel_inc, float t0,
+                          float deltaT, const bpgb_options *opt);
+
+/* ---- plans on device buffers --------------------------------------------
+ * host_pairs: the pair list on the host (analysed once; copied to the device).
+ * execute: d_H is a device array [P, h_pitch] of opt->h_dtype; d_volume is a device
+ * float (or interleaved complex64 for C64) array [Nx, Ny, Nz] that is overwritten.
+ * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream); allocates
+ * nothing, so it can be captured in a CUDA graph. */
+int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_pairs,
+                     uint32_t T, const uint32_t *voxels_per_side,
+                     const float *volume_zero_pos, const float *voxel_inc, float t0,
+                     float deltaT, const bpgb_options *opt);
+int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *stream);
+/* Synchronises the plan's last stream and reports device-side diagnostics: returns
+ * BPGB_ERR_TIMEOUT if a bounded wait gave up, BPGB_ERR_WINDOW if checked mode counted
+ * out-of-window bins (count in *violations when non-null), else BPGB_OK. */
+int bpgb_plan_check(bpgb_plan plan, uint64_t *violations);
+int bpgb_plan_get_info(bpgb_plan plan, bpgb_plan_info *info);
+/* Bin indices the plan's algorithm uses for voxels h_voxel_ids[0..n) and every pair:
+ * d_bins[i * P + p] (int32, -1 = outside [0, T)).  For parity measurement only. */
+int bpgb_plan_dump_bins(bpgb_plan plan, const int64_t *h_voxel_ids, int64_t n,
+                        int32_t *d_bins, void *stream);
+int bpgb_plan_destroy(bpgb_plan plan);
+
+/* Failure-path probe: a one-warp kernel waits, with the pipeline's bounded wait, on an
+ * mbarrier that nothing arrives on.  Returns BPGB_ERR_TIMEOUT once `spin_limit` polls ran
+ * out (the device stays usable), so callers and tests can check the timeout path. */
+int bpgb_diag_wait_timeout(uint32_t spin_limit);
+
+/* ---- phasor pulse --------------------------------------------------------
+ * d_out[r, t] = sum_k d_H[r, t + k - K/2] * (cos_k, sin_k), read index in (0, T), with
+ * K = int(times * wavelength / deltaT) taps built as the reference does (FP64 Gaussian
+ * and phase, rounded to FP32).  d_H: float [rows, in_pitch]; d_out: interleaved
+ * complex64 [rows, out_pitch].  Asynchronous on stream. */
+int bpgb_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch,
+                      float wavelength, float deltaT, uint32_t times, float *d_out,
+                      uint32_t out_pitch, void *stream);
+/* The K taps (cos then sin, 2*K floats) of the pulse; returns K (taps may be NULL). */
+int bpgb_phasor_taps(float wavelength, float deltaT, uint32_t times, float *taps, int cap);
+
+/* ---- geometry ------------------------------------------------------------
+ * Pair list and wall legs computed on the GPU in FP64 (rounded to FP32 fields).
+ * Grids are host arrays [gx, gy, 3] row-major.  confocal != 0: P = cx*cy and the
+ * laser point is the camera point.  out_pairs: host array of P pairs. */
+int bpgb_precompute_pairs(const float *laser_position, const float *laser_grid, uint32_t lx,
+                          uint32_t ly, const float *camera_position, const float *camera_grid,
+                          uint32_t cx, uint32_t cy, int confocal, bpgb_pair *out_pairs);
+/* zero = position - size/2; inc rows = axis * size / (n - 1) with axes x, y, z (or the
+ * wall-aligned basis y = -normal, x = y cross z, z = y cross x when wall_normal != 0). */
+int bpgb_volume_basis(const float *volume_position, const float *volume_size,
+                      const uint32_t *voxels_per_side, const float *wall_normal,
+                      float *volume_zero_pos, float *voxel_inc);
+/* First and last time index any voxel can reach, +-100 bins, as fractional indices
+ * (min over corners of the laser grid, camera grid and volume; see DESIGN notes). */
+int bpgb_time_limits(const float *laser_position, const float *laser_grid, uint32_t lx,
+                     uint32_t ly, const float *camera_position, const float *camera_grid,
+                     uint32_t cx, uint32_t cy, const float *volume_position,
+                     const float *volume_size, float t0, float deltaT, float *min_index,
+                     float *max_index);
+
+/* ---- whole reconstructions (host buffers) --------------------------------
+ * bp::backproject / bp::phasor_reconstruction on the GPU: time-window crop, FP64 pair
+ * precompute, basis, then the backprojection.  transient_data is row-major
+ * [lx, ly, cx, cy, T] (exhaustive) or [cx, cy, T] (confocal).  t0_mode 0 keeps the
+ * reference's fractional chunk offset (chunked_t0 = t0 + m*deltaT with m unfloored),
+ * 1 uses the floored offset (no sub-bin shift).  Output [Nx, Ny, Nz] float, or
+ * interleaved complex64 for the phasor call. */
+int bpgb_backproject_capture(const float *transient_data, uint32_t T,
+                             const float *camera_grid, uint32_t cx, uint32_t cy,
+                             const float *laser_grid, uint32_t lx, uint32_t ly,
+                             const float *camera_position, const float *laser_position,
+                             float t0, float deltaT, int confocal,
+                             const float *volume_position, const float *volume_size,
+                             const uint32_t *voxels_per_side, const float *wall_normal,
+                             int t0_mode, const bpgb_options *opt, float *out_volume);
+int bpgb_phasor_capture(const float *transient_data, uint32_t T, const float *camera_grid,
+                        uint32_t cx, uint32_t cy, const float *laser_grid, uint32_t lx,
+                        uint32_t ly, const float *camera_position, const float *laser_position,
+                        float t0, float deltaT, int confocal, const float *volume_position,
+                        const float *volume_size, const uint32_t *voxels_per_side,
+                        const float *wall_normal, float wavelength, const bpgb_options *opt,
+                        float *out_volume);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BACKPROJECTOR_GB300_H */

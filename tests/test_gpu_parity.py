@@ -1,0 +1,394 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference kernel's outputs
+(golden fixtures) and the FP64 CPU oracle.
+
+Tolerances (vs the FP64 oracle, on real-valued renderings):
+  EXACT  rel-L2 <= 2e-3: FP32 geometry flips ~0.1% of bins (the reference's own rate);
+  FAST   rel-L2 <= 5e-3 for FP32/Kahan/BF16-free FP16 rows, mis-binned fraction <= 1%;
+against the reference kernel (golden): integer-valued H -> bit-identical volumes.
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from backprojector_gb300 import capi, synthetic
+from oracle import oracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+pytestmark = pytest.mark.gpu
+
+
+def golden(name):
+    p = GOLDEN / f"{name}.npz"
+    if not p.exists():
+        pytest.skip(f"golden fixture {name} not generated")
+    z = np.load(p)
+    d = {k: z[k] for k in z.files}
+    d["pairs"] = np.ascontiguousarray(d["pairs"]).view(capi.PAIR_DTYPE).reshape(-1)
+    if str(d.get("H_kind", "")) == "ramp":
+        T = int(d["T"])
+        d["H"] = np.broadcast_to(np.arange(1, T + 1, dtype=np.float32), (len(d["pairs"]), T)).copy()
+    return d
+
+
+def run_plan(cuda, H, pairs, N, zero, inc, t0, dT, **opt):
+    import torch
+
+    cplx = np.iscomplexobj(H)
+    dtype = opt.get("h_dtype", capi.DTYPE_C64 if cplx else capi.DTYPE_F32)
+    opt["h_dtype"] = dtype
+    Hn = np.ascontiguousarray(H)
+    if dtype == capi.DTYPE_F16:
+        dH = torch.from_numpy(Hn.astype(np.float32)).to(cuda).half()
+    elif dtype == capi.DTYPE_BF16:
+        dH = torch.from_numpy(Hn.astype(np.float32)).to(cuda).bfloat16()
+    elif cplx:
+        dH = torch.from_numpy(Hn.astype(np.complex64)).to(cuda)
+    else:
+        dH = torch.from_numpy(Hn.astype(np.float32)).to(cuda)
+    shape = tuple(int(v) for v in N)
+    dV = torch.full(shape, float("nan"), dtype=torch.complex64 if cplx else torch.float32,
+                    device=cuda)
+    with capi.Plan(pairs, H.shape[-1], N, zero, inc, t0, dT, **opt) as plan:
+        plan.execute(dH, dV)
+        viol = plan.check()
+        info = plan.info()
+        out = dV.cpu().numpy()
+    return out, info, viol
+
+
+# ---------------------------------------------------------------- vs the reference kernel
+
+@pytest.mark.parametrize("name", ["exhaustive_p256_n16", "single_p256_n24", "single_ramp_n24"])
+def test_exact_bit_identical_to_reference_kernel(cuda, name):
+    g = golden(name)
+    out, info, _ = run_plan(cuda, g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                            float(g["dT"]), algo=capi.ALGO_EXACT)
+    assert info["algo"] == "exact"
+    # integer-valued H: every partial sum is exact, so equal bins <=> equal volumes
+    assert np.array_equal(out, g["ref_volume"]), np.abs(out - g["ref_volume"]).max()
+
+
+def test_exact_float_rows_vs_reference_kernel(cuda):
+    g = golden("objects_p256_n20")
+    out, _, _ = run_plan(cuda, g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                         float(g["dT"]), algo=capi.ALGO_EXACT)
+    # same bins, different summation order only
+    assert oracle.rel_l2(out, g["ref_volume"]) < 1e-6
+
+
+def test_exact_complex_vs_reference_kernel(cuda):
+    g = golden("complex_p64_n16")
+    out, _, _ = run_plan(cuda, g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                         float(g["dT"]), algo=capi.ALGO_EXACT)
+    assert oracle.rel_l2(out, g["ref_volume"]) < 1e-6
+
+
+def test_ragged_pairs_reference_drops_tail(cuda):
+    """P = 300: the reference loops i < P / blockDim and ignores the last 44 pairs
+    (backproject_cuda.cu:150); this engine uses all of them."""
+    g = golden("ragged_p300_n16")
+    block = int(g["ref_block"])
+    kept = (len(g["pairs"]) // block) * block
+    assert kept < len(g["pairs"])
+    out_kept, _, _ = run_plan(cuda, g["H"][:kept], g["pairs"][:kept], g["N"], g["zero"], g["inc"],
+                              float(g["t0"]), float(g["dT"]), algo=capi.ALGO_EXACT)
+    assert np.array_equal(out_kept, g["ref_volume"])
+    out_all, _, _ = run_plan(cuda, g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                             float(g["dT"]), algo=capi.ALGO_EXACT)
+    ref_all = oracle.bp_gpu_f64(g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                                float(g["dT"]))
+    assert oracle.rel_l2(out_all, ref_all) < 2e-3
+
+
+def test_n40_every_voxel_visited(cuda):
+    """N = 40 (not a multiple of 16): the reference's voxel cursor wraps
+    (backproject_cuda.cu:65-80) and recomputes some voxels; every voxel it writes matches
+    this engine exactly."""
+    g = golden("single_p64_n40")
+    out, _, _ = run_plan(cuda, g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                         float(g["dT"]), algo=capi.ALGO_EXACT)
+    seen = oracle.reference_visited(g["N"])
+    assert np.array_equal(out[seen], g["ref_volume"][seen])
+    assert np.all(g["ref_volume"][~seen] == 0)
+    ref = oracle.bp_gpu_f64(g["H"], g["pairs"], g["N"], g["zero"], g["inc"], float(g["t0"]),
+                            float(g["dT"]))
+    assert oracle.rel_l2(out, ref) < 2e-3
+
+
+# ---------------------------------------------------------------- vs the FP64 oracle
+
+CASES = [
+    ("dense_exhaustive_16", dict(laser_grid=(4, 4), spad_grid=(8, 8), voxels=16)),
+    ("precision_64", dict()),
+    ("octree_256", dict()),
+]
+
+
+def _cap(name, kw, seed=5):
+    return synthetic.make_capture(name, seed=seed, small=True, **kw)
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_exact_vs_fp64_oracle_and_misbinned(cuda, name, kw):
+    import torch
+
+    c = _cap(name, kw)
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    out, _, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                         algo=capi.ALGO_EXACT)
+    assert oracle.rel_l2(out, ref) < 2e-3
+    ids = np.random.default_rng(0).choice(c.nvox, size=min(64, c.nvox), replace=False)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_EXACT) as plan:
+        d = torch.empty((len(ids), c.P), dtype=torch.int32, device=cuda)
+        plan.dump_bins(ids, d)
+        gpu_bins = d.cpu().numpy()
+    b64 = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT, ids, 0)
+    b32 = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT, ids, 1)
+    assert oracle.misbinned_fraction(gpu_bins, b64) < 5e-3
+    # the CPU FP32 emulation differs from norm3df only next to .5 boundaries
+    assert oracle.misbinned_fraction(gpu_bins, b32) < 1e-3
+
+
+FAST_VARIANTS = [
+    dict(h_dtype=capi.DTYPE_F32, accum=capi.ACCUM_F32),
+    dict(h_dtype=capi.DTYPE_F32, accum=capi.ACCUM_KAHAN),
+    dict(h_dtype=capi.DTYPE_F16, accum=capi.ACCUM_F32),
+    dict(h_dtype=capi.DTYPE_BF16, accum=capi.ACCUM_KAHAN),
+]
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+@pytest.mark.parametrize("var", FAST_VARIANTS, ids=["f32", "kahan", "f16", "bf16kahan"])
+def test_fast_vs_fp64_oracle(cuda, name, kw, var):
+    c = _cap(name, kw)
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    H = c.H
+    scale = 1.0
+    if var["h_dtype"] in (capi.DTYPE_F16, capi.DTYPE_BF16):
+        scale = float(np.abs(H).max()) / 1024.0 or 1.0
+        H = H / scale
+    out, info, viol = run_plan(cuda, H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                               algo=capi.ALGO_FAST, checked=1, h_scale=scale, **var)
+    assert info["algo"] == "fast"
+    assert viol == 0
+    tol = {capi.DTYPE_F32: 5e-3, capi.DTYPE_F16: 6e-3, capi.DTYPE_BF16: 2e-2}[var["h_dtype"]]
+    assert oracle.rel_l2(out, ref) < tol
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_fast_misbinned_fraction(cuda, name, kw):
+    import torch
+
+    c = _cap(name, kw)
+    ids = np.random.default_rng(1).choice(c.nvox, size=min(64, c.nvox), replace=False)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST) as plan:
+        d = torch.empty((len(ids), c.P), dtype=torch.int32, device=cuda)
+        plan.dump_bins(ids, d)
+        gpu_bins = d.cpu().numpy()
+    b64 = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT, ids, 0)
+    assert oracle.misbinned_fraction(gpu_bins, b64) < 1e-2
+
+
+def test_fast_matches_its_own_bin_dump(cuda):
+    """The FAST volume equals the sum of H at the bins its dump reports (same arithmetic)."""
+    import torch
+
+    c = _cap("precision_64", {})
+    out, _, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                         algo=capi.ALGO_FAST)
+    ids = np.arange(0, c.nvox, 97)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST) as plan:
+        d = torch.empty((len(ids), c.P), dtype=torch.int32, device=cuda)
+        plan.dump_bins(ids, d)
+        b = d.cpu().numpy()
+    rows = np.arange(c.P)[None, :]
+    vals = np.where(b >= 0, c.H[rows, np.clip(b, 0, c.T - 1)], 0.0).astype(np.float64).sum(1)
+    assert np.allclose(out.ravel()[ids], vals, rtol=1e-5, atol=1e-3)
+
+
+def test_fast_complex_vs_oracle(cuda):
+    c = _cap("phasor_128", {})
+    Hc = oracle.phasor_pulse(c.H, c.wavelength, c.deltaT)
+    ref = oracle.bp_gpu_c64(Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    out, info, viol = run_plan(cuda, Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                               algo=capi.ALGO_FAST, checked=1)
+    assert info["algo"] == "fast" and viol == 0
+    assert oracle.rel_l2(out, ref) < 5e-3
+
+
+def test_confocal_fast_vs_oracle(cuda):
+    c = synthetic.make_capture("precision_64", seed=7, small=True, confocal=True)
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    out, info, viol = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                               c.deltaT, algo=capi.ALGO_FAST, checked=1)
+    assert info["geometry"] == "confocal" and viol == 0
+    assert oracle.rel_l2(out, ref) < 5e-3
+
+
+@pytest.mark.parametrize("splits", [1, 3, 7])
+def test_fast_pair_splits_deterministic(cuda, splits):
+    c = _cap("precision_64", {})
+    a, ia, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                        algo=capi.ALGO_FAST, pair_splits=splits)
+    b, _, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                       algo=capi.ALGO_FAST, pair_splits=splits)
+    assert ia["pair_splits"] == splits
+    assert np.array_equal(a, b)
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    assert oracle.rel_l2(a, ref) < 5e-3
+
+
+@pytest.mark.parametrize("tile", list(range(6)))
+def test_fast_tile_presets(cuda, tile):
+    c = _cap("octree_256", {})
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    out, info, viol = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                               c.deltaT, algo=capi.ALGO_FAST, tile=tile, checked=1)
+    assert viol == 0
+    assert oracle.rel_l2(out, ref) < 5e-3
+
+
+# ---------------------------------------------------------------- other kernels
+
+def test_phasor_pulse_bit_identical_to_oracle(cuda):
+    import torch
+
+    c = _cap("phasor_128", {})
+    ref = oracle.phasor_pulse(c.H, c.wavelength, c.deltaT)
+    dH = torch.from_numpy(c.H).to(cuda)
+    dO = torch.empty(c.H.shape, dtype=torch.complex64, device=cuda)
+    capi.phasor_pulse_device(dH, c.P, c.T, c.T, c.wavelength, c.deltaT, dO, c.T)
+    torch.cuda.synchronize()
+    assert np.array_equal(dO.cpu().numpy(), ref)
+
+
+def test_pairs_fp64_bit_identical(cuda):
+    c = _cap("dense_exhaustive_16", dict(laser_grid=(4, 4), spad_grid=(8, 8), voxels=16))
+    got = capi.precompute_pairs(c.laser_position, c.laser_grid, c.camera_position, c.camera_grid)
+    ref = oracle.precompute_distances(c.laser_position, c.laser_grid, c.camera_position,
+                                      c.camera_grid)
+    assert got.tobytes() == ref.tobytes()
+    assert got.tobytes() == c.pairs.tobytes()
+
+
+def test_dropin_host_call_matches_plan(cuda):
+    c = _cap("precision_64", {})
+    a = capi.backproject_host(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                              algo=capi.ALGO_EXACT)
+    b, _, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                       algo=capi.ALGO_EXACT)
+    assert np.array_equal(a, b)
+    # ragged T (not a multiple of 4): the host call pads rows for the TMA path
+    H = np.ascontiguousarray(c.H[:, :1021])
+    f = capi.backproject_host(H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    ref = oracle.bp_gpu_f64(H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    assert oracle.rel_l2(f, ref) < 5e-3
+
+
+def test_empty_and_out_of_range(cuda):
+    c = _cap("precision_64", {})
+    empty = capi.backproject_host(np.zeros((0, c.T), np.float32), c.pairs[:0], c.voxels_per_side,
+                                  c.zero, c.inc, c.t0, c.deltaT)
+    assert np.all(empty == 0)
+    # every bin beyond T: the volume is zero on both paths
+    for algo in (capi.ALGO_EXACT, capi.ALGO_FAST):
+        out = capi.backproject_host(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0 + 100.0,
+                                    c.deltaT, algo=algo)
+        assert np.all(out == 0)
+    ones = np.ones_like(c.H)
+    out = capi.backproject_host(ones, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                                algo=capi.ALGO_EXACT)
+    b = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                    np.arange(c.nvox), 1)
+    # all-ones H: each voxel counts its in-range pairs
+    assert np.abs(out.ravel() - (b >= 0).sum(1)).max() <= 2
+
+
+def test_errors_are_status_codes(cuda):
+    c = _cap("precision_64", {})
+    bad = c.pairs.copy()
+    bad["camera_point"][3, 1] = np.nan
+    with pytest.raises(capi.BackprojectorError) as e:
+        capi.backproject_host(c.H, bad, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    assert e.value.status == capi.ERR_INVALID_ARGUMENT
+    L = capi.lib()
+    n = np.asarray(c.voxels_per_side, np.uint32)
+    out = np.zeros(c.nvox, np.float32)
+    st = L.bpgb_backproject_f32(capi.vptr(c.H), c.H.size - 1, c.T, capi.vptr(c.pairs), c.P,
+                                capi.vptr(out), capi.u32ptr(n), capi.fptr(c.zero), capi.fptr(c.inc),
+                                c.t0, c.deltaT)
+    assert st == capi.ERR_INVALID_ARGUMENT
+    with pytest.raises(capi.BackprojectorError) as e:
+        capi.backproject_host(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                              algo=capi.ALGO_EXACT, h_dtype=capi.DTYPE_F16)
+    assert e.value.status == capi.ERR_UNSUPPORTED
+
+
+def test_bounded_wait_reports_timeout(cuda):
+    """A wait on a barrier nothing arrives on gives up and reports; the context stays
+    usable for the next call."""
+    assert capi.lib().bpgb_diag_wait_timeout(64) == capi.ERR_TIMEOUT
+    c = _cap("precision_64", {})
+    out = capi.backproject_host(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    assert np.isfinite(out).all()
+
+
+# ---------------------------------------------------------------- whole reconstructions
+
+def test_nlosbpy_backproject_matches_oracle_pipeline(cuda):
+    from backprojector_gb300 import load_nlosbpy
+
+    nl = load_nlosbpy()
+    c = _cap("dense_exhaustive_16", dict(laser_grid=(4, 4), spad_grid=(8, 8), voxels=16))
+    vol = nl.backproject(c.transient_array(), c.camera_grid, c.laser_grid, c.camera_position,
+                         c.laser_position, c.t0, c.deltaT, False, c.volume_position, c.volume_size,
+                         c.voxels_per_side, np.zeros(3, np.float32), assume_row_major=True)
+    m, M = capi.time_limits(c.laser_position, c.laser_grid, c.camera_position, c.camera_grid,
+                            c.volume_position, c.volume_size, c.t0, c.deltaT)
+    lo, hi = int(np.floor(m)), int(np.ceil(M))
+    chunk = np.zeros((c.P, hi - lo), np.float32)
+    s0, s1 = max(lo, 0), min(c.T, hi)
+    chunk[:, s0 - lo:s1 - lo] = c.H[:, s0:s1]
+    ct0 = np.float32(c.t0) + np.float32(m) * np.float32(c.deltaT)
+    ref = oracle.bp_gpu_f64(chunk, c.pairs, c.voxels_per_side, c.zero, c.inc, float(ct0), c.deltaT)
+    assert vol.shape == tuple(c.voxels_per_side)
+    assert oracle.rel_l2(vol, ref) < 5e-3
+    # column-major inputs (the binding's default) are the same arrays with axes reversed
+    vol_cm = nl.backproject(c.transient_array().T, c.camera_grid.T, c.laser_grid.T,
+                            c.camera_position, c.laser_position, c.t0, c.deltaT, False,
+                            c.volume_position, c.volume_size, c.voxels_per_side,
+                            np.zeros(3, np.float32))
+    assert np.array_equal(vol_cm, vol)
+    with pytest.raises(Exception):
+        nl.backproject(c.transient_array(), c.camera_grid, c.laser_grid, c.camera_position,
+                       c.laser_position, c.t0, c.deltaT, False, c.volume_position, c.volume_size,
+                       c.voxels_per_side, np.zeros(3, np.float32), assume_row_major=True,
+                       use_cpu=True)
+
+
+def test_nlosbpy_phasor_matches_oracle_pipeline(cuda):
+    from backprojector_gb300 import load_nlosbpy
+
+    nl = load_nlosbpy()
+    c = _cap("phasor_128", {})
+    vol = nl.phasor(c.transient_array(), c.camera_grid, c.laser_grid, c.camera_position,
+                    c.laser_position, c.t0, c.deltaT, False, c.volume_position, c.volume_size,
+                    c.voxels_per_side, c.wavelength, assume_row_major=True)
+    m, M = capi.time_limits(c.laser_position, c.laser_grid, c.camera_position, c.camera_grid,
+                            c.volume_position, c.volume_size, c.t0, c.deltaT)
+    lo, hi = int(m), int(M)
+    chunk = np.zeros((c.P, hi - lo), np.float32)
+    s0, s1 = max(lo, 0), min(c.T, hi)
+    chunk[:, s0 - lo:s1 - lo] = c.H[:, s0:s1]
+    Hc = oracle.phasor_pulse(chunk, c.wavelength, c.deltaT)
+    ct0 = np.float32(c.t0) + np.float32(lo) * np.float32(c.deltaT)
+    ref = oracle.bp_gpu_c64(Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, float(ct0), c.deltaT)
+    assert vol.dtype == np.complex64
+    assert oracle.rel_l2(vol, ref) < 5e-3
