@@ -160,6 +160,12 @@ def test_oracle_pinned_to_reference_kernel_outputs():
             continue
         emu = oracle.bp_gpu_f32emu(H, pairs, *args, ref_block=block)
         o64 = oracle.bp_gpu_f64(H, pairs, *args, ref_block=block)
-        assert oracle.rel_l2(emu[mask], ref[mask]) < 1e-4, f.name
+        if np.all(H == np.round(H)):
+            # integer rows: sums are exact, so a voxel differs only where one of its
+            # updates is binned differently (norm3df vs the correctly rounded norm next
+            # to a .5 boundary): at most 0.1% of voxels
+            assert np.mean(emu[mask] != ref[mask]) <= 1e-3, f.name
+        else:
+            assert oracle.rel_l2(emu[mask], ref[mask]) < 1e-4, f.name
         assert oracle.rel_l2(o64[mask], ref[mask]) < 2e-2, f.name
         assert np.all(ref[~mask] == 0), f.name
