@@ -87,6 +87,8 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
     "bpgb_plan_destroy": (C.c_int, [_P]),
     "bpgb_diag_wait_timeout": (C.c_int, [C.c_uint32]),
+    "bpgb_backproject_noalloc": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64, C.c_uint64,
+                                           C.c_int, _U32, _F, _F, C.c_float, C.c_float, _P, _P]),
     "bpgb_phasor_pulse": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
                                     C.c_uint32, _P, C.c_uint32, _P]),
     "bpgb_phasor_taps": (C.c_int, [C.c_float, C.c_float, C.c_uint32, _F, C.c_int]),

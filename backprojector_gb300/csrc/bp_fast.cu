@@ -867,3 +867,305 @@ void fast_plan_free(FastPlan *fp) {
 }
 
 }  // namespace bpgb
+
+// ==================================================================================
+// Allocation-free entry point (bpgb_backproject_noalloc).
+//
+// For callers that cannot allocate device memory at call time -- code running under a
+// custom or pre-sized memory pool, host integrations whose allocator is owned by someone
+// else, long-running services that forbid cudaMalloc after start-up.  The call runs the
+// same FAST kernel as bpgb_plan_execute (FP32 rows, FP32 sums), but everything it needs
+// beyond the caller's input and output buffers lives in one file-scope device array:
+// the SPAD / laser tables (built on the GPU from the caller's device pair list), the
+// diagnostic counters, and the per-split partial sums.  Nothing is allocated on the
+// device or the host heap.
+// ==================================================================================
+namespace bpgb {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)BPGB_NOALLOC_SCRATCH_BYTES;
+constexpr size_t kNoAllocDiagBytes = 256;  // counters; the tables start 256 B in
+
+// Shared by every call of every thread of the process on a given device.  The host
+// never names it directly as a pointer: its device address comes from
+// cudaGetSymbolAddress (noalloc_scratch_ptr below).
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+struct NoAllocTableArgs {
+    double u[3][3];
+    double zero[3];
+    double dT, t0;
+    uint64_t L, S;
+    int confocal;
+};
+
+__device__ __forceinline__ void frame_fp64(const NoAllocTableArgs &t, const float *pt, double o[3]) {
+    const double d0 = __dsub_rn((double)pt[0], t.zero[0]);
+    const double d1 = __dsub_rn((double)pt[1], t.zero[1]);
+    const double d2 = __dsub_rn((double)pt[2], t.zero[2]);
+    for (int r = 0; r < 3; r++)
+        o[r] = __dadd_rn(__dadd_rn(__dmul_rn(t.u[r][0], d0), __dmul_rn(t.u[r][1], d1)),
+                         __dmul_rn(t.u[r][2], d2));
+}
+
+__device__ __forceinline__ bool same_point(const float *a, const float *b) {
+    return __float_as_uint(a[0]) == __float_as_uint(b[0]) &&
+           __float_as_uint(a[1]) == __float_as_uint(b[1]) &&
+           __float_as_uint(a[2]) == __float_as_uint(b[2]);
+}
+
+// Tables of the FAST kernel from a device pair list (same FP64 arithmetic as the plan's
+// host build), plus a check that the list has the stated order p = l * S + s (or is
+// confocal): diag[2] counts pairs that break it, diag[3] non-finite values.
+__global__ void noalloc_tables_kernel(const bpgb_pair *__restrict__ pairs, const NoAllocTableArgs t,
+                                      float4 *__restrict__ tab, unsigned long long *__restrict__ diag) {
+    const uint64_t P = t.L * t.S;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const bpgb_pair pr = pairs[p];
+        const uint64_t l = p / t.S, s = p % t.S;
+        const float *f = reinterpret_cast<const float *>(&pr);
+        bool finite = true;
+        for (int k = 0; k < 8; k++) finite = finite && isfinite(f[k]);
+        if (!finite) atomicAdd(&diag[3], 1ull);
+        bool ok;
+        if (t.confocal) {
+            ok = same_point(pr.laser_point, pr.camera_point) &&
+                 __float_as_uint(pr.laser_wall) == __float_as_uint(pr.camera_wall);
+        } else {
+            const bpgb_pair &head = pairs[l * t.S];
+            const bpgb_pair &col = pairs[s];
+            ok = same_point(pr.laser_point, head.laser_point) &&
+                 __float_as_uint(pr.laser_wall) == __float_as_uint(head.laser_wall) &&
+                 same_point(pr.camera_point, col.camera_point) &&
+                 __float_as_uint(pr.camera_wall) == __float_as_uint(col.camera_wall);
+        }
+        if (!ok) atomicAdd(&diag[2], 1ull);
+        if (l == 0) {
+            double g[3];
+            frame_fp64(t, pr.camera_point, g);
+            const double cs = t.confocal
+                                  ? __ddiv_rn(__dadd_rn((double)pr.camera_wall, (double)pr.laser_wall), t.dT)
+                                  : __ddiv_rn((double)pr.camera_wall, t.dT);
+            tab[s] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)cs);
+        }
+        if (s == 0) {
+            double g[3] = {0.0, 0.0, 0.0};
+            double c = __ddiv_rn(-t.t0, t.dT);
+            if (!t.confocal) {
+                frame_fp64(t, pr.laser_point, g);
+                c = __dadd_rn(c, __ddiv_rn((double)pr.laser_wall, t.dT));
+            }
+            tab[t.S + l] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)c);
+        }
+    }
+}
+
+// Device address of g_noalloc_scratch, resolved once per device with that device
+// current (the symbol's host-side name is only a stand-in, never a device pointer).
+int noalloc_scratch_ptr(unsigned char **out) {
+    static std::mutex mu;
+    static unsigned char *ptrs[64] = {nullptr};
+    int dev = 0;
+    BPGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(BPGB_ERR_UNSUPPORTED, "device index >= 64");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(no-alloc scratch)");
+        ptrs[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = ptrs[dev];
+    return BPGB_OK;
+}
+
+}  // namespace
+}  // namespace bpgb
+
+using namespace bpgb;
+
+extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h_pitch,
+                                        const bpgb_pair *d_pairs, uint64_t num_lasers,
+                                        uint64_t num_spads, int confocal,
+                                        const uint32_t *voxels_per_side,
+                                        const float *volume_zero_pos, const float *voxel_inc,
+                                        float t0, float deltaT, float *d_volume, void *stream) {
+    clear_error();
+    if (!d_H || !d_pairs || !d_volume || !voxels_per_side || !volume_zero_pos || !voxel_inc)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    if (T == 0 || num_lasers == 0 || num_spads < 2 || (confocal && num_lasers != 1))
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         "need T > 0, num_spads >= 2 and num_lasers >= 1 (1 when confocal)");
+    const uint32_t pitch = h_pitch ? h_pitch : T;
+    if (pitch < T || (pitch * 4ull) % 16 || ((uintptr_t)d_H) % 16)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         "H must be 16-byte aligned with a row pitch that is a multiple of 4");
+    if (!std::isfinite(t0) || !(deltaT > 0.0f) || !std::isfinite(deltaT))
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "t0 / deltaT must be finite, deltaT > 0");
+    const uint64_t P = num_lasers * num_spads;
+    if (P >= (1ull << 31) || T >= (1u << 30))
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "P or T too large for TMA coordinates");
+    const uint64_t tab_bytes = (num_spads + num_lasers) * sizeof(float4);
+    if (kNoAllocDiagBytes + tab_bytes > kNoAllocScratchBytes)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         "lasers + SPADs need " + std::to_string(kNoAllocDiagBytes + tab_bytes) +
+                             " bytes of scratch; the no-alloc limit is " +
+                             std::to_string(kNoAllocScratchBytes) + " bytes");
+    Volume vol{};
+    for (int k = 0; k < 3; k++) {
+        vol.n[k] = voxels_per_side[k];
+        vol.zero[k] = volume_zero_pos[k];
+        if (!std::isfinite(vol.zero[k]))
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "volume_zero_pos is not finite");
+    }
+    for (int k = 0; k < 9; k++) {
+        vol.inc[k] = voxel_inc[k];
+        if (!std::isfinite(vol.inc[k]))
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "voxel_inc is not finite");
+    }
+    if (vol.count() == 0) return BPGB_OK;
+    double u[3][3], hd[3];
+    if (!volume_frame(vol, u, hd))
+        return set_error(BPGB_ERR_UNSUPPORTED, "voxel basis is not orthogonal");
+    if (!encode_fn()) return set_error(BPGB_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    int sms = 0;
+    int st = require_device(&sms);
+    if (st) return st;
+    unsigned char *scratch = nullptr;
+    st = noalloc_scratch_ptr(&scratch);
+    if (st) return st;
+
+    // Launch arguments: the default tile preset of the FAST kernel, FP32 rows.
+    const FastConfig cfg = fast_preset(-1, BPGB_DTYPE_F32);
+    FastArgs a{};
+    for (int k = 0; k < 3; k++) a.n[k] = vol.n[k];
+    a.lane[0] = cfg.lx;
+    a.lane[1] = cfg.ly;
+    a.lane[2] = cfg.lz;
+    a.warp[0] = cfg.wx;
+    a.warp[1] = cfg.wy;
+    a.warp[2] = cfg.wz;
+    for (int k = 0; k < 3; k++) {
+        a.tdim[k] = cfg.tile(k);
+        a.tiles[k] = (vol.n[k] + a.tdim[k] - 1) / a.tdim[k];
+    }
+    const double dT = deltaT;
+    const double sb = (confocal ? 2.0 : 1.0) / dT, sa = confocal ? 0.0 : 1.0 / dT;
+    a.sb = (float)sb;
+    a.sa = (float)sa;
+    for (int k = 0; k < 3; k++) {
+        a.h[k] = (float)hd[k];
+        a.hs[k] = (float)(hd[k] * sb);
+    }
+    a.L = num_lasers;
+    a.S = num_spads;
+    a.T = T;
+    a.out_scale = 1.0f;
+    a.nvox = vol.count();
+    a.spin_limit = 1u << 22;
+    double diag2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+        const double e = (double)(a.tdim[k] - 1) * hd[k];
+        diag2 += e * e;
+    }
+    const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
+    const uint32_t esz = 4;
+    a.align = 16 / esz;
+    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
+    const uint32_t bw_align = 128 / esz;
+    a.nbox = (w_need + 255) / 256;
+    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
+    if (a.BW > 256) return set_error(BPGB_ERR_UNSUPPORTED, "window box too wide");
+    a.W = a.BW * a.nbox;
+    a.row_bytes = a.W * esz;
+    const uint32_t budget = 200 * 1024;
+    uint32_t chunk = (uint32_t)std::min<uint64_t>(std::min<uint32_t>(cfg.chunk, kMaxChunk), num_spads);
+    uint32_t stages = std::min<uint32_t>(cfg.stages, 8);
+    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
+    while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
+    while (stages > 2 && stages * stage_bytes(chunk) > budget) stages--;
+    if (stages * stage_bytes(chunk) > budget)
+        return set_error(BPGB_ERR_UNSUPPORTED, "time window of one tile does not fit in shared memory");
+    a.chunk = chunk;
+    a.stages = stages;
+    a.stage_bytes = stage_bytes(chunk);
+    a.nchunks = (uint32_t)((num_spads + chunk - 1) / chunk);
+    const uint32_t threads = 32 * (1 + cfg.wx * cfg.wy * cfg.wz);
+    const uint32_t smem = a.stages * a.stage_bytes + 128;
+    void *kern = select_kernel(BPGB_DTYPE_F32, false, false);
+    BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    BPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)threads, smem));
+    if (occ < 1) return set_error(BPGB_ERR_UNSUPPORTED, "fast kernel does not fit on an SM");
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    const uint64_t items = a.L * a.nchunks;
+    uint64_t splits = 1;
+    const uint64_t want = 2ull * sms * occ;
+    if (ntiles < want) splits = (want + ntiles - 1) / ntiles;
+    // partial sums must fit next to the tables: fewer splits, never an error
+    const uint64_t part_off = (kNoAllocDiagBytes + tab_bytes + 255) / 256 * 256;
+    const uint64_t part_room = kNoAllocScratchBytes - std::min<uint64_t>(kNoAllocScratchBytes, part_off);
+    const uint64_t max_splits = part_room / (a.nvox * sizeof(float));
+    splits = std::max<uint64_t>(1, std::min<uint64_t>({splits, items, max_splits}));
+    if (ntiles * splits >= (1ull << 31)) return set_error(BPGB_ERR_UNSUPPORTED, "grid too large");
+    a.splits = (uint32_t)splits;
+
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long *diag = reinterpret_cast<unsigned long long *>(scratch);
+    float4 *tab = reinterpret_cast<float4 *>(scratch + kNoAllocDiagBytes);
+    float *partial = reinterpret_cast<float *>(scratch + part_off);
+    // The array keeps the previous call's contents: the counters must start at zero.
+    BPGB_CUDA_TRY(cudaMemsetAsync(diag, 0, kNoAllocDiagBytes, s));
+    NoAllocTableArgs ta{};
+    for (int r = 0; r < 3; r++)
+        for (int k = 0; k < 3; k++) ta.u[r][k] = u[r][k];
+    for (int k = 0; k < 3; k++) ta.zero[k] = (double)vol.zero[k];
+    ta.dT = dT;
+    ta.t0 = (double)t0;
+    ta.L = num_lasers;
+    ta.S = num_spads;
+    ta.confocal = confocal ? 1 : 0;
+    const unsigned tblocks = (unsigned)std::min<uint64_t>((P + 255) / 256, 152ull * 16);
+    noalloc_tables_kernel<<<tblocks, 256, 0, s>>>(d_pairs, ta, tab, diag);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    // A pair list with non-finite values or another order never reaches the window
+    // arithmetic of the main kernel.
+    unsigned long long h[4] = {0, 0, 0, 0};
+    BPGB_CUDA_TRY(cudaMemcpyAsync(h, diag, sizeof(h), cudaMemcpyDeviceToHost, s));
+    BPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[3]) return set_error(BPGB_ERR_INVALID_ARGUMENT, std::to_string(h[3]) + " non-finite pair values");
+    if (h[2])
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         std::to_string(h[2]) + " pairs break the stated lasers x SPADs order");
+
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {T, P};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * esz};
+    const cuuint32_t box[2] = {a.BW, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(d_H), dims,
+                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    void *target = a.splits > 1 ? (void *)partial : (void *)d_volume;
+    const float4 *spads = tab;
+    const float4 *lasers = tab + num_spads;
+    void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target, (void *)&diag,
+                    (void *)&a};
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3((unsigned)(ntiles * splits)), dim3(threads), args, smem, s));
+    count_launches(1);
+    if (a.splits > 1) {
+        const unsigned blocks = (unsigned)std::min<uint64_t>((a.nvox + 255) / 256, 152ull * 8);
+        reduce_splits_kernel<false, false><<<blocks, 256, 0, s>>>(partial, d_volume, a.nvox,
+                                                                 a.splits, 1.0f);
+        count_launches(1);
+        BPGB_CUDA_TRY(cudaGetLastError());
+    }
+    BPGB_CUDA_TRY(cudaMemcpyAsync(h, diag, sizeof(h), cudaMemcpyDeviceToHost, s));
+    BPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[0]) return set_error(BPGB_ERR_TIMEOUT, std::to_string(h[0]) + " device waits timed out");
+    return BPGB_OK;
+}

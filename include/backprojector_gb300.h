@@ -164,6 +164,35 @@ int bpgb_plan_dump_bins(bpgb_plan plan, const int64_t *h_voxel_ids, int64_t n,
                         int32_t *d_bins, void *stream);
 int bpgb_plan_destroy(bpgb_plan plan);
 
+/* ---- allocation-free backprojection ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory
+ * when they reconstruct: services running under a fixed, pre-sized memory pool,
+ * host applications whose GPU allocator belongs to another framework, code that must
+ * not call cudaMalloc / cudaFree after start-up.  Computes the same volume as a
+ * FAST-algorithm plan (FP32 rows, FP32 sums) without allocating anything on the device
+ * or the host heap: its working memory (SPAD / laser tables built on the GPU from
+ * d_pairs, diagnostic counters, per-split partial sums) is one static device array of
+ * BPGB_NOALLOC_SCRATCH_BYTES that every GPU which loads this library holds until the
+ * process exits.
+ *   d_H       device FP32 rows [P, h_pitch] (h_pitch 0 = T), 16-byte aligned, h_pitch a
+ *             multiple of 4; P = num_lasers * num_spads
+ *   d_pairs   device pair list in the order p = l * num_spads + s (precompute_distances
+ *             order), or confocal (num_lasers = 1, laser point = camera point)
+ *   d_volume  device float [Nx, Ny, Nz], overwritten
+ * Lists whose tables need more than the array (16 * (num_lasers + num_spads) + 256
+ * bytes > BPGB_NOALLOC_SCRATCH_BYTES) are rejected with BPGB_ERR_INVALID_ARGUMENT; for
+ * large volumes it uses fewer pair splits so the partial sums fit.  The call is
+ * synchronous on `stream`.  The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress) for that device: make it before any stream capture.
+ * Every call shares the one array and overwrites it, so calls that overlap on the GPU
+ * (other threads, other streams) race: serialise them. */
+#define BPGB_NOALLOC_SCRATCH_BYTES (16u << 20)
+int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h_pitch,
+                             const bpgb_pair *d_pairs, uint64_t num_lasers, uint64_t num_spads,
+                             int confocal, const uint32_t *voxels_per_side,
+                             const float *volume_zero_pos, const float *voxel_inc, float t0,
+                             float deltaT, float *d_volume, void *stream);
+
 /* Failure-path probe: a one-warp kernel waits, with the pipeline's bounded wait, on an
  * mbarrier that nothing arrives on.  Returns BPGB_ERR_TIMEOUT once `spin_limit` polls ran
  * out (the device stays usable), so callers and tests can check the timeout path. */
