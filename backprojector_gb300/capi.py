@@ -38,7 +38,7 @@ class Options(C.Structure):
     _fields_ = [("algo", C.c_int32), ("h_dtype", C.c_int32), ("accum", C.c_int32),
                 ("h_pitch", C.c_uint32), ("h_scale", C.c_float), ("tile", C.c_int32),
                 ("pair_splits", C.c_int32), ("checked", C.c_int32), ("spin_limit", C.c_uint32),
-                ("reserved", C.c_int32 * 7)]
+                ("chunk", C.c_int32), ("stages", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class PlanInfo(C.Structure):
@@ -87,6 +87,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
     "bpgb_plan_destroy": (C.c_int, [_P]),
     "bpgb_diag_wait_timeout": (C.c_int, [C.c_uint32]),
+    "bpgb_diag_pipe_rates": (C.c_int, [C.POINTER(C.c_double)]),
     "bpgb_backproject_noalloc": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, C.c_uint64, C.c_uint64,
                                            C.c_int, _U32, _F, _F, C.c_float, C.c_float, _P, _P]),
     "bpgb_phasor_pulse": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
@@ -165,6 +166,13 @@ def options(**kw) -> Options:
             raise TypeError(f"unknown option {k}")
         setattr(o, k, v)
     return o
+
+
+def pipe_rates() -> dict:
+    """Measured per-SM per-clock rates: rsqrt results, FP32 lanes (packed FMA), shared loads."""
+    r = (C.c_double * 3)()
+    check(lib().bpgb_diag_pipe_rates(r), "bpgb_diag_pipe_rates")
+    return {"rsqrt_per_sm_clk": r[0], "fp32_lanes_per_sm_clk": r[1], "lds_per_sm_clk": r[2]}
 
 
 def launch_count() -> int:

@@ -7,22 +7,25 @@
 // or are confocal (:399-413, laser point = camera point, d = 2|v - c| + 2 cw).
 //
 // Work decomposition
-//   * A CTA owns one voxel tile (tdim = lane layout x warp layout, K voxels per thread
-//     along z) and, when `splits` > 1, a contiguous range of (laser, SPAD-chunk) items.
+//   * A CTA owns one voxel tile and, when `splits` > 1, a contiguous range of
+//     (laser, SPAD-chunk) items.  Each consumer thread holds K voxels on a line along
+//     one axis (`kax`); a warp's lanes cover the other axes at each step of that line.
 //   * Warp 0 is the producer.  For every item it computes, per SPAD row of the chunk,
 //     the range of bins the tile can reach (exact distance bounds from the SPAD and
-//     the laser point to the tile's box), aligns it for TMA, writes a row record
-//     (SPAD position relative to the tile centre in bin units, row constant) and
-//     issues 2-D TMA tile loads of H[p, lo : lo + W] into a shared-memory stage.  Out-
-//     of-range bins (< 0 or >= T) arrive as zeros from the TMA unit, which is exactly
-//     the reference's "skip out-of-range bins" rule.
-//   * Warps 1..n are consumers.  Each thread keeps K voxels in registers: the laser leg
-//     A_k = |v_k - l| / dT + lw / dT - t0 / dT (recomputed per laser), the voxel's
-//     coordinates relative to the tile centre (bin units) and the K accumulators.  Per
-//     row and voxel:  q = |v - c|^2 (2 ops), rsqrt (MUFU), x = q * rsqrt(q) + A_k,
-//     + row constant, + 1.5*2^23 (round to nearest), gather from shared memory at
-//     the rounded index, accumulate (9 issue slots; FP16/BF16 rows use the one-op
-//     mixed-precision add).
+//     the laser point to the tile's box), aligns it for TMA, writes a 32-byte row record
+//     (SPAD position relative to the tile centre in bin units, row constant, pre-splatted
+//     for packed FP32x2 arithmetic) and issues 2-D TMA tile loads of H[p, lo : lo + W]
+//     into a shared-memory stage.  Out-of-range bins (< 0 or >= T) arrive as zeros from
+//     the TMA unit, which is exactly the reference's "skip out-of-range bins" rule.
+//   * Warps 1..n are consumers.  Per thread: the laser leg A_k = |v_k - l| / dT +
+//     lw / dT - t0 / dT (recomputed per laser), the voxels' coordinates relative to the
+//     tile centre (bin units) and the accumulators, all as voxel pairs.  Per row and
+//     voxel pair (sm_100 packed FP32x2 ops, one instruction for two voxels):
+//       dz = vk - ck; q = dz*dz + D; r = rsqrt(q) (MUFU, per voxel);
+//       x = q*r + A; y = x + row constant; z = y + 1.5*2^23 (round to nearest);
+//     then one shifted-add per voxel forms the shared address and one load gathers.
+//     That is 6 FP32x2 + 2 MUFU + 2 address + 2 gathers = 12 issue slots per two updates;
+//     FP16/BF16 rows accumulate with sm_100's one-op mixed-precision add.
 //   * Stages are handed over with mbarriers (full: TMA bytes + producer arrive; empty:
 //     one arrive per consumer warp).  Every wait is bounded; a wait that gives up sets
 //     an error counter the host reads (bpgb_plan_check) and the CTA drains its own
@@ -51,9 +54,10 @@ namespace bpgb {
 namespace {
 
 constexpr uint32_t kMaxChunk = 32;
-constexpr uint32_t kTableBytes = kMaxChunk * 16;  // float4 per row
-constexpr float kMargin = 2.0f;                   // bins of slack around each window
-constexpr float kQEps = 1e-6f;                    // keeps q > 0 (bins^2)
+constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
+constexpr uint32_t kTableBytes = kMaxChunk * kRecordBytes;
+constexpr float kMargin = 2.0f;                            // bins of slack around each window
+constexpr float kQEps = 1e-6f;                             // keeps q > 0 (bins^2)
 
 struct FastArgs {
     uint32_t n[3];      // voxels per side
@@ -61,6 +65,8 @@ struct FastArgs {
     uint32_t tdim[3];   // tile size in voxels
     uint32_t lane[3];   // lane layout (product 32)
     uint32_t warp[3];   // consumer warp layout
+    uint32_t kax;       // axis of each thread's voxel line
+    uint32_t oax0, oax1;  // the two other axes
     float h[3];         // voxel step length along each frame axis (m)
     float hs[3];        // h * sb (bins)
     float sb;           // SPAD-leg scale: 1/dT (2/dT confocal)
@@ -120,10 +126,10 @@ __device__ __forceinline__ void box_bounds(const FastArgs &a, const TileGeo &g, 
 }
 
 // Row record of SPAD entry G (frame position, row constant Cs) for a tile and laser Lt:
-// e = (c' relative to the tile centre in bin units, Cs - lo); returns lo (the window's
-// first bin, aligned down to a.align).
+// e[a] = SPAD coordinate a relative to the tile centre in bin units, ew = Cs - lo;
+// returns lo, the window's first bin, aligned down to a.align.
 __device__ __forceinline__ int32_t row_record(const FastArgs &a, const TileGeo &g, float4 G,
-                                              float4 Lt, float4 &e) {
+                                              float4 Lt, float e[3], float &ew) {
     float dmin, dmax, lmin, lmax;
     box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
     box_bounds(a, g, Lt.x, Lt.y, Lt.z, lmin, lmax);
@@ -131,67 +137,59 @@ __device__ __forceinline__ int32_t row_record(const FastArgs &a, const TileGeo &
     int32_t lo = (int32_t)floorf(bmin - kMargin);
     const int32_t al = (int32_t)a.align;
     lo -= ((lo % al) + al) % al;
-    e.x = __fmul_rn(G.x - __fmul_rn(g.ctr[0], a.h[0]), a.sb);
-    e.y = __fmul_rn(G.y - __fmul_rn(g.ctr[1], a.h[1]), a.sb);
-    e.z = __fmul_rn(G.z - __fmul_rn(g.ctr[2], a.h[2]), a.sb);
-    e.w = G.w - (float)lo;
+    const float gp[3] = {G.x, G.y, G.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) e[k] = __fmul_rn(gp[k] - __fmul_rn(g.ctr[k], a.h[k]), a.sb);
+    ew = G.w - (float)lo;
     return lo;
 }
 
-// Laser leg of voxel (ix, iy, iz) for laser entry Lt = (frame position, lw/dT - t0/dT).
-__device__ __forceinline__ float laser_leg(const FastArgs &a, uint32_t ix, uint32_t iy,
-                                           uint32_t iz, float4 Lt) {
-    const float dx = __fmaf_rn((float)ix, a.h[0], -Lt.x);
-    const float dy = __fmaf_rn((float)iy, a.h[1], -Lt.y);
-    const float dz = __fmaf_rn((float)iz, a.h[2], -Lt.z);
+// Laser leg of voxel idx[3] for laser entry Lt = (frame position, lw/dT - t0/dT).
+__device__ __forceinline__ float laser_leg(const FastArgs &a, const uint32_t idx[3], float4 Lt) {
+    const float dx = __fmaf_rn((float)idx[0], a.h[0], -Lt.x);
+    const float dy = __fmaf_rn((float)idx[1], a.h[1], -Lt.y);
+    const float dz = __fmaf_rn((float)idx[2], a.h[2], -Lt.z);
     const float d = sqrtf(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))));
     return __fmaf_rn(a.sa, d, Lt.w);
 }
 
-__device__ __forceinline__ float rel_coord(const FastArgs &a, const TileGeo &g, int k,
+// x_i for i = 0, 1, 2 without indexing a local array (runtime axis choices would
+// otherwise place small arrays in local memory).
+template <typename T>
+__device__ __forceinline__ T sel3(T x0, T x1, T x2, uint32_t i) {
+    return i == 0 ? x0 : (i == 1 ? x1 : x2);
+}
+
+__device__ __forceinline__ float rel_coord(const FastArgs &a, const TileGeo &g, uint32_t ax,
                                            uint32_t idx) {
-    return __fmul_rn((float)idx - g.ctr[k], a.hs[k]);
+    return __fmul_rn((float)idx - sel3(g.ctr[0], g.ctr[1], g.ctr[2], ax),
+                     sel3(a.hs[0], a.hs[1], a.hs[2], ax));
 }
 
-// D = dx^2 + dy^2 + eps for one row, shared by the thread's K voxels.
-__device__ __forceinline__ float row_dxy(float vx, float vy, float4 e) {
-    const float dx = vx - e.x, dy = vy - e.y;
-    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, kQEps));
+// D = d0^2 + d1^2 + eps over the two axes across a thread's voxel line.
+__device__ __forceinline__ float row_d(float v0, float v1, float e0, float e1) {
+    const float d0 = v0 - e0, d1 = v1 - e1;
+    return __fmaf_rn(d0, d0, __fmaf_rn(d1, d1, kQEps));
 }
 
-// Index into the row's window (as the float bits of x + 1.5*2^23).
-__device__ __forceinline__ uint32_t window_bits(float vz, float D, float A, float4 e) {
-    const float dz = vz - e.z;
+// Window index (as float bits of x + 1.5*2^23) of one voxel; the scalar form of the
+// packed consumer arithmetic, used by the bin dump.
+__device__ __forceinline__ uint32_t window_bits(float vk, float D, float A, float ek, float ew) {
+    const float dz = __fadd_rn(vk, -ek);
     const float q = __fmaf_rn(dz, dz, D);
     const float r = rsqrt_approx(q);
-    const float x = __fmaf_rn(q, r, A);
-    const float y = __fadd_rn(x, e.w);
+    const float y = __fmaf_rn(q, r, __fadd_rn(A, ew));
     return __float_as_uint(__fadd_rn(y, kMagic));
 }
 
-template <typename HT>
-__device__ __forceinline__ void store_out(void *out, uint64_t i, const Acc<HT> &acc,
-                                          float scale);
-template <>
-__device__ __forceinline__ void store_out<float>(void *out, uint64_t i, const Acc<float> &acc,
-                                                 float scale) {
-    ((float *)out)[i] = acc.v * scale;
-}
-template <>
-__device__ __forceinline__ void store_out<__half>(void *out, uint64_t i,
-                                                  const Acc<__half> &acc, float scale) {
-    ((float *)out)[i] = acc.v * scale;
-}
-template <>
-__device__ __forceinline__ void store_out<__nv_bfloat16>(void *out, uint64_t i,
-                                                         const Acc<__nv_bfloat16> &acc,
-                                                         float scale) {
-    ((float *)out)[i] = acc.v * scale;
-}
-template <>
-__device__ __forceinline__ void store_out<float2>(void *out, uint64_t i, const Acc<float2> &acc,
-                                                  float scale) {
-    ((float2 *)out)[i] = make_float2(acc.v.x * scale, acc.v.y * scale);
+// ---- shared-memory gathers ------------------------------------------------------------
+// Plain loads at a byte offset from the dynamic shared-memory base: the compiler sees them
+// as shared-memory reads, keeps them between the stage's full-barrier wait and its
+// empty-barrier arrive (asm with memory clobbers) and is free to interleave the
+// independent voxel chains in between.
+template <typename T>
+__device__ __forceinline__ T lds(const unsigned char *smem, uint32_t off) {
+    return *reinterpret_cast<const T *>(smem + off);
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
@@ -201,14 +199,107 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
     sum = t;
 }
 
+// Accumulators of one voxel pair, per storage type.
+template <typename HT>
+struct Pair;
+
+template <>
+struct Pair<float> {
+    static constexpr uint32_t kEsz = 4, kShift = 2;
+    float2 a;
+    __device__ __forceinline__ void zero() { a = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
+        const float v0 = lds<float>(sm, p0), v1 = lds<float>(sm, p1);
+        a = __fadd2_rn(a, make_float2(v0, v1));
+    }
+    __device__ __forceinline__ void fold(Pair &comp, const Pair &part) {
+        kahan_add(a.x, comp.a.x, part.a.x);
+        kahan_add(a.y, comp.a.y, part.a.y);
+    }
+    __device__ __forceinline__ void finish(const Pair &comp) {
+        a.x -= comp.a.x;
+        a.y -= comp.a.y;
+    }
+    __device__ __forceinline__ void store(void *out, uint64_t i, int which, float s) const {
+        ((float *)out)[i] = (which ? a.y : a.x) * s;
+    }
+};
+
+template <int IS_BF16>
+struct PairHalf {
+    static constexpr uint32_t kEsz = 2, kShift = 1;
+    float2 a;
+    __device__ __forceinline__ void zero() { a = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
+        const unsigned short h0 = lds<unsigned short>(sm, p0), h1 = lds<unsigned short>(sm, p1);
+        if (IS_BF16) {
+            asm("add.rn.f32.bf16 %0, %1, %0;" : "+f"(a.x) : "h"(h0));
+            asm("add.rn.f32.bf16 %0, %1, %0;" : "+f"(a.y) : "h"(h1));
+        } else {
+            asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(a.x) : "h"(h0));
+            asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(a.y) : "h"(h1));
+        }
+    }
+    __device__ __forceinline__ void fold(PairHalf &comp, const PairHalf &part) {
+        kahan_add(a.x, comp.a.x, part.a.x);
+        kahan_add(a.y, comp.a.y, part.a.y);
+    }
+    __device__ __forceinline__ void finish(const PairHalf &comp) {
+        a.x -= comp.a.x;
+        a.y -= comp.a.y;
+    }
+    __device__ __forceinline__ void store(void *out, uint64_t i, int which, float s) const {
+        ((float *)out)[i] = (which ? a.y : a.x) * s;
+    }
+};
+template <>
+struct Pair<__half> : PairHalf<0> {};
+template <>
+struct Pair<__nv_bfloat16> : PairHalf<1> {};
+
+template <>
+struct Pair<float2> {
+    static constexpr uint32_t kEsz = 8, kShift = 3;
+    float2 a0, a1;
+    __device__ __forceinline__ void zero() { a0 = a1 = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
+        const float2 v0 = lds<float2>(sm, p0), v1 = lds<float2>(sm, p1);
+        a0 = __fadd2_rn(a0, v0);
+        a1 = __fadd2_rn(a1, v1);
+    }
+    __device__ __forceinline__ void fold(Pair &comp, const Pair &part) {
+        kahan_add(a0.x, comp.a0.x, part.a0.x);
+        kahan_add(a0.y, comp.a0.y, part.a0.y);
+        kahan_add(a1.x, comp.a1.x, part.a1.x);
+        kahan_add(a1.y, comp.a1.y, part.a1.y);
+    }
+    __device__ __forceinline__ void finish(const Pair &comp) {
+        a0.x -= comp.a0.x;
+        a0.y -= comp.a0.y;
+        a1.x -= comp.a1.x;
+        a1.y -= comp.a1.y;
+    }
+    __device__ __forceinline__ void store(void *out, uint64_t i, int which, float s) const {
+        const float2 v = which ? a1 : a0;
+        ((float2 *)out)[i] = make_float2(v.x * s, v.y * s);
+    }
+};
+
+// Resident CTAs per SM each variant is compiled for: K = 8 two CTAs (18 warps, 96
+// registers; three CTAs at 72 registers measured 2% slower on the 256^3 capture),
+// K = 16 one CTA with room for its 16 chains.
+__host__ __device__ constexpr int fast_ctas_per_sm(int k, bool kahan, int esz) {
+    return (void)kahan, (void)esz, k == 16 ? 1 : 2;
+}
+
 template <typename HT, int K, bool KAHAN, bool CHECKED>
-__global__ void __launch_bounds__(288, 1)
+__global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
     bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
                    const float4 *__restrict__ lasers, void *__restrict__ out,
                    unsigned long long *__restrict__ diag, const FastArgs a) {
-    using AccT = Acc<HT>;
-    using Elem = typename AccT::Elem;
-    constexpr uint32_t esz = AccT::kBytes;
+    using PairT = Pair<HT>;
+    constexpr uint32_t esz = PairT::kEsz;
+    constexpr int NP = K / 2;
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[8];
@@ -264,7 +355,8 @@ __global__ void __launch_bounds__(288, 1)
             if (*(volatile int *)&abort_flag) break;
             const uint64_t l = it / a.nchunks;
             const uint64_t s0 = (it % a.nchunks) * a.chunk;
-            const uint32_t nrows = (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
+            const uint32_t nrows =
+                (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
             unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
             float4 *table = reinterpret_cast<float4 *>(st);
             const uint32_t data = smem_addr(st + kTableBytes);
@@ -273,9 +365,12 @@ __global__ void __launch_bounds__(288, 1)
             if (lane < nrows) {
                 const float4 G = spads[s0 + lane];
                 const float4 Lt = lasers[l];
-                float4 e;
-                lo = row_record(a, g, G, Lt, e);
-                table[lane] = e;
+                float e[3], ew;
+                lo = row_record(a, g, G, Lt, e, ew);
+                const float ek = sel3(e[0], e[1], e[2], a.kax);
+                table[2 * lane] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
+                                              sel3(e[0], e[1], e[2], a.oax1), 0.0f, 0.0f);
+                table[2 * lane + 1] = make_float4(-ek, -ek, ew, ew);
             }
             __syncwarp();
             if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
@@ -305,27 +400,34 @@ __global__ void __launch_bounds__(288, 1)
 
     // ---------------- consumers ----------------
     const uint32_t cw = warp - 1;
-    const uint32_t lxi = lane % a.lane[0], lyi = (lane / a.lane[0]) % a.lane[1];
-    const uint32_t lzi = lane / (a.lane[0] * a.lane[1]);
-    const uint32_t wxi = cw % a.warp[0], wyi = (cw / a.warp[0]) % a.warp[1];
-    const uint32_t wzi = cw / (a.warp[0] * a.warp[1]);
-    const uint32_t ix = g.org[0] + wxi * a.lane[0] + lxi;
-    const uint32_t iy = g.org[1] + wyi * a.lane[1] + lyi;
-    const uint32_t iz0 = g.org[2] + wzi * a.lane[2] * K + lzi;
-    const float vx = rel_coord(a, g, 0, ix), vy = rel_coord(a, g, 1, iy);
-    float vz[K], A[K];
+    const uint32_t li[3] = {lane % a.lane[0], (lane / a.lane[0]) % a.lane[1],
+                            lane / (a.lane[0] * a.lane[1])};
+    const uint32_t wi[3] = {cw % a.warp[0], (cw / a.warp[0]) % a.warp[1],
+                            cw / (a.warp[0] * a.warp[1])};
+    const uint32_t bx = g.org[0] + wi[0] * a.lane[0] * (a.kax == 0 ? K : 1) + li[0];
+    const uint32_t by = g.org[1] + wi[1] * a.lane[1] * (a.kax == 1 ? K : 1) + li[1];
+    const uint32_t bz = g.org[2] + wi[2] * a.lane[2] * (a.kax == 2 ? K : 1) + li[2];
+    const uint32_t bk = sel3(bx, by, bz, a.kax);
+    const uint32_t kstep = sel3(a.lane[0], a.lane[1], a.lane[2], a.kax);
+    const float v0 = rel_coord(a, g, a.oax0, sel3(bx, by, bz, a.oax0));
+    const float v1 = rel_coord(a, g, a.oax1, sel3(bx, by, bz, a.oax1));
+    float2 vk[NP], A[NP];
 #pragma unroll
-    for (int k = 0; k < K; k++) vz[k] = rel_coord(a, g, 2, iz0 + k * a.lane[2]);
+    for (int i = 0; i < NP; i++) {
+        vk[i].x = rel_coord(a, g, a.kax, bk + (2 * i) * kstep);
+        vk[i].y = rel_coord(a, g, a.kax, bk + (2 * i + 1) * kstep);
+    }
 
-    AccT acc[K];
-    float comp[K][2];
+    PairT acc[NP], comp[NP];
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        acc[k].zero();
-        comp[k][0] = comp[k][1] = 0.0f;
+    for (int i = 0; i < NP; i++) {
+        acc[i].zero();
+        comp[i].zero();
     }
     uint64_t cur_l = ~0ull;
     uint32_t violations = 0;
+    const float2 magic2 = make_float2(kMagic, kMagic);
+    const uint32_t row_elems = a.row_bytes / esz;
 
     for (uint64_t it = i0; it < i1; it++) {
         const uint64_t i = it - i0;
@@ -335,7 +437,19 @@ __global__ void __launch_bounds__(288, 1)
         if (l != cur_l) {
             const float4 Lt = lasers[l];
 #pragma unroll
-            for (int k = 0; k < K; k++) A[k] = laser_leg(a, ix, iy, iz0 + k * a.lane[2], Lt);
+            for (int p = 0; p < NP; p++) {
+#pragma unroll
+                for (int w = 0; w < 2; w++) {
+                    const uint32_t kv = bk + (2 * p + w) * kstep;
+                    const uint32_t idx[3] = {a.kax == 0 ? kv : bx, a.kax == 1 ? kv : by,
+                                             a.kax == 2 ? kv : bz};
+                    const float v = laser_leg(a, idx, Lt);
+                    if (w == 0)
+                        A[p].x = v;
+                    else
+                        A[p].y = v;
+                }
+            }
             cur_l = l;
         }
         // Every lane acquires the stage (TMA bytes and the producer's row records).
@@ -349,77 +463,82 @@ __global__ void __launch_bounds__(288, 1)
             break;
         }
         const uint64_t s0 = (it % a.nchunks) * a.chunk;
-        const uint32_t nrows = (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
+        const uint32_t nrows =
+            (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
         const unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
         const float4 *table = reinterpret_cast<const float4 *>(st);
-        const Elem *data = reinterpret_cast<const Elem *>(st + kTableBytes);
-        const uint32_t row_elems = a.row_bytes / esz;
+        const uint32_t data = pad + stage * a.stage_bytes + kTableBytes;  // offset from smem_raw
 
-        AccT part[K];
+        PairT part[NP];
         if (KAHAN) {
 #pragma unroll
-            for (int k = 0; k < K; k++) part[k].zero();
+            for (int p = 0; p < NP; p++) part[p].zero();
         }
+        // Two rows per iteration give each warp 2 x NP independent voxel-pair chains
+        // (one for complex rows, whose accumulators already double the registers).
+#pragma unroll(PairT::kEsz == 8 ? 1 : 2)
         for (uint32_t j = 0; j < nrows; j++) {
-            const float4 e = table[j];
-            const float D = row_dxy(vx, vy, e);
-            const uint32_t rbase = j * row_elems - kMagicBits;
+            const float4 r0 = table[2 * j];
+            const float4 r1 = table[2 * j + 1];
+            const float D = row_d(v0, v1, r0.x, r0.y);
+            const float2 D2 = make_float2(D, D);
+            const float2 nk = make_float2(r1.x, r1.y);
+            const float2 ew = make_float2(r1.z, r1.w);
+            const uint32_t rbase = data + j * a.row_bytes - kMagicBits * esz;
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                uint32_t idx = window_bits(vz[k], D, A[k], e) + rbase;
+            for (int p = 0; p < NP; p++) {
+                // laser leg + row constant ahead of the rsqrt: one dependent op after it
+                const float2 Ae = __fadd2_rn(A[p], ew);
+                const float2 dz = __fadd2_rn(vk[p], nk);
+                const float2 q = __ffma2_rn(dz, dz, D2);
+                const float2 r = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+                const float2 y = __ffma2_rn(q, r, Ae);
+                const float2 z = __fadd2_rn(y, magic2);
+                uint32_t b0 = __float_as_uint(z.x), b1 = __float_as_uint(z.y);
                 if (CHECKED) {
-                    const uint32_t rel = idx - j * row_elems;
-                    if (rel >= a.W) {
+                    const uint32_t r0i = b0 - kMagicBits, r1i = b1 - kMagicBits;
+                    if (r0i >= a.W) {
                         violations++;
-                        idx = j * row_elems + ((int32_t)rel < 0 ? 0u : a.W - 1);
+                        b0 = kMagicBits + ((int32_t)r0i < 0 ? 0u : a.W - 1);
+                    }
+                    if (r1i >= a.W) {
+                        violations++;
+                        b1 = kMagicBits + ((int32_t)r1i < 0 ? 0u : a.W - 1);
                     }
                 }
+                const uint32_t p0 = rbase + (b0 << PairT::kShift);
+                const uint32_t p1 = rbase + (b1 << PairT::kShift);
                 if (KAHAN)
-                    part[k].add(data, idx);
+                    part[p].gather2(smem_raw, p0, p1);
                 else
-                    acc[k].add(data, idx);
+                    acc[p].gather2(smem_raw, p0, p1);
             }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&empty_bar[stage]));
         if (KAHAN) {
 #pragma unroll
-            for (int k = 0; k < K; k++) {
-                if constexpr (sizeof(acc[k].v) == 8) {
-                    float2 pv = *reinterpret_cast<float2 *>(&part[k].v);
-                    float2 &av = *reinterpret_cast<float2 *>(&acc[k].v);
-                    kahan_add(av.x, comp[k][0], pv.x);
-                    kahan_add(av.y, comp[k][1], pv.y);
-                } else {
-                    float &av = *reinterpret_cast<float *>(&acc[k].v);
-                    kahan_add(av, comp[k][0], *reinterpret_cast<float *>(&part[k].v));
-                }
-            }
+            for (int p = 0; p < NP; p++) acc[p].fold(comp[p], part[p]);
         }
+        (void)row_elems;
     }
     if (CHECKED && violations) atomicAdd(&diag[1], (unsigned long long)violations);
     if (KAHAN) {
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            if constexpr (sizeof(acc[k].v) == 8) {
-                float2 &av = *reinterpret_cast<float2 *>(&acc[k].v);
-                av.x -= comp[k][0];
-                av.y -= comp[k][1];
-            } else {
-                float &av = *reinterpret_cast<float *>(&acc[k].v);
-                av -= comp[k][0];
-            }
-        }
+        for (int p = 0; p < NP; p++) acc[p].finish(comp[p]);
     }
-    if (ix >= a.n[0] || iy >= a.n[1]) return;
     const float scale = a.splits > 1 ? 1.0f : a.out_scale;
     const uint64_t part_off = a.splits > 1 ? (uint64_t)split * a.nvox : 0;
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-        const uint32_t iz = iz0 + k * a.lane[2];
-        if (iz < a.n[2])
-            store_out<HT>(out, part_off + ((uint64_t)ix * a.n[1] + iy) * a.n[2] + iz, acc[k],
-                          scale);
+    for (int p = 0; p < NP; p++) {
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            const uint32_t kv = bk + (2 * p + w) * kstep;
+            const uint32_t x = a.kax == 0 ? kv : bx, y = a.kax == 1 ? kv : by,
+                           z = a.kax == 2 ? kv : bz;
+            if (x < a.n[0] && y < a.n[1] && z < a.n[2])
+                acc[p].store(out, part_off + ((uint64_t)x * a.n[1] + y) * a.n[2] + z, w, scale);
+        }
     }
 }
 
@@ -455,22 +574,24 @@ __global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
          w += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i = w / P, p = w % P;
         const int64_t id = ids[i];
-        const uint32_t iz = (uint32_t)(id % a.n[2]);
-        const uint32_t iy = (uint32_t)((id / a.n[2]) % a.n[1]);
-        const uint32_t ix = (uint32_t)(id / ((int64_t)a.n[1] * a.n[2]));
-        const uint32_t tile = ((iy / a.tdim[1]) * a.tiles[0] + ix / a.tdim[0]) * a.tiles[2] +
-                              iz / a.tdim[2];
+        const uint32_t idx[3] = {(uint32_t)(id / ((int64_t)a.n[1] * a.n[2])),
+                                 (uint32_t)((id / a.n[2]) % a.n[1]), (uint32_t)(id % a.n[2])};
+        const uint32_t tile =
+            ((idx[1] / a.tdim[1]) * a.tiles[0] + idx[0] / a.tdim[0]) * a.tiles[2] +
+            idx[2] / a.tdim[2];
         TileGeo g;
         tile_of_block(a, tile, g);
         const uint64_t l = p / a.S, s = p % a.S;
         const float4 Lt = lasers[l];
-        float4 e;
-        const int32_t lo = row_record(a, g, spads[s], Lt, e);
-        const float A = laser_leg(a, ix, iy, iz, Lt);
-        const float vx = rel_coord(a, g, 0, ix), vy = rel_coord(a, g, 1, iy);
-        const float vz = rel_coord(a, g, 2, iz);
-        const float D = row_dxy(vx, vy, e);
-        const int32_t rel = (int32_t)(window_bits(vz, D, A, e) - kMagicBits);
+        float e[3], ew;
+        const int32_t lo = row_record(a, g, spads[s], Lt, e, ew);
+        const float A = laser_leg(a, idx, Lt);
+        const float v0 = rel_coord(a, g, a.oax0, sel3(idx[0], idx[1], idx[2], a.oax0));
+        const float v1 = rel_coord(a, g, a.oax1, sel3(idx[0], idx[1], idx[2], a.oax1));
+        const float vk = rel_coord(a, g, a.kax, sel3(idx[0], idx[1], idx[2], a.kax));
+        const float D = row_d(v0, v1, sel3(e[0], e[1], e[2], a.oax0), sel3(e[0], e[1], e[2], a.oax1));
+        const float ek = sel3(e[0], e[1], e[2], a.kax);
+        const int32_t rel = (int32_t)(window_bits(vk, D, A, ek, ew) - kMagicBits);
         const int32_t b = lo + rel;
         bins[w] = (b >= 0 && b < (int32_t)a.T) ? b : -1;
     }
@@ -530,15 +651,143 @@ CUtensorMapDataType tma_type(int dt) {
     }
 }
 
-// Tile presets: {lx, ly, lz, k, wx, wy, wz, chunk, stages}.
+int encode_rows(CUtensorMap *map, int dtype, const void *d_H, uint32_t T, uint64_t P,
+                uint32_t pitch, uint32_t box) {
+    const uint32_t esz = dtype_bytes(dtype);
+    const cuuint64_t dims[2] = {T, P};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * esz};
+    const cuuint32_t boxd[2] = {box, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_fn()(map, tma_type(dtype), 2, const_cast<void *>(d_H), dims, strides, boxd,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return BPGB_OK;
+}
+
+// Tile presets: {lx, ly, lz, k, wx, wy, wz, kaxis, chunk, stages}.  The voxel line of a
+// thread runs along `kaxis`; lanes cover the other two axes.
 const FastConfig kPresets[] = {
-    {8, 4, 1, 8, 2, 2, 2, 32, 4},  // 16 x 8 x 16 tile, 2048 voxels
-    {4, 4, 2, 8, 4, 2, 1, 32, 4},  // 16 x 8 x 16, z pairs per lane
-    {8, 4, 1, 8, 2, 1, 4, 32, 4},  // 16 x 4 x 32
-    {4, 8, 1, 8, 2, 2, 2, 32, 4},  // 8 x 16 x 16
-    {8, 4, 1, 8, 1, 2, 4, 16, 4},  // 8 x 8 x 32
-    {8, 4, 1, 8, 2, 2, 2, 16, 3},  // 16 x 8 x 16, shallower stages
+    {8, 1, 4, 8, 2, 1, 4, 1, 32, 4},  // 16 x 8 x 16, lanes over x-z, lines along y (depth)
+    {8, 4, 1, 8, 2, 2, 2, 2, 32, 4},  // 16 x 8 x 16, lanes over x-y, lines along z
+    {4, 1, 8, 8, 4, 1, 2, 1, 32, 4},  // 16 x 8 x 16, 4 x 8 lane blocks over x-z
+    {8, 1, 4, 8, 2, 2, 2, 1, 32, 4},  // 16 x 16 x 8
+    {8, 1, 4, 8, 4, 1, 2, 1, 32, 4},  // 32 x 8 x 8
+    {4, 1, 8, 8, 2, 1, 4, 1, 32, 4},  // 8 x 8 x 32
+    {8, 1, 4, 8, 1, 2, 4, 1, 32, 4},  // 8 x 16 x 16
+    {8, 1, 4, 16, 2, 1, 4, 1, 32, 4}, // 16 x 16 x 16, 16 voxels per thread
+    {8, 1, 4, 16, 1, 1, 8, 1, 32, 4}, // 8 x 16 x 32, 16 voxels per thread
+    {4, 1, 8, 16, 2, 1, 4, 1, 32, 4}, // 8 x 16 x 32, 4 x 8 lane blocks
 };
+
+template <typename HT, int K>
+void *kernel_ptr(bool kahan, bool checked) {
+    if (kahan)
+        return checked ? (void *)bp_fast_kernel<HT, K, true, true>
+                       : (void *)bp_fast_kernel<HT, K, true, false>;
+    return checked ? (void *)bp_fast_kernel<HT, K, false, true>
+                   : (void *)bp_fast_kernel<HT, K, false, false>;
+}
+
+// K = 16 (twice the independent chains per thread) is built for the real row types;
+// complex rows keep K = 8 (twice the accumulator registers).
+void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k) {
+    const bool k16 = k == 16;
+    switch (dtype) {
+        case BPGB_DTYPE_F16:
+            return k16 ? kernel_ptr<__half, 16>(kahan, checked) : kernel_ptr<__half, 8>(kahan, checked);
+        case BPGB_DTYPE_BF16:
+            return k16 ? kernel_ptr<__nv_bfloat16, 16>(kahan, checked)
+                       : kernel_ptr<__nv_bfloat16, 8>(kahan, checked);
+        case BPGB_DTYPE_C64: return kernel_ptr<float2, 8>(kahan, checked);
+        default:
+            return k16 ? kernel_ptr<float, 16>(kahan, checked) : kernel_ptr<float, 8>(kahan, checked);
+    }
+}
+
+// Launch arguments of the fast kernel for a volume, pair factorisation and tile preset:
+// everything but the pair splits.  No allocation.  chunk / stages > 0 override the
+// preset; otherwise the chunk shrinks until the stages fit the shared-memory budget.
+int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const double hd[3],
+              bool confocal, double dT, double t0, uint64_t L, uint64_t S, uint32_t T,
+              uint32_t esz, bool kahan, uint32_t chunk_req, uint32_t stages_req,
+              std::string *why) {
+    auto no = [&](const std::string &m) {
+        if (why) *why = m;
+        return BPGB_ERR_UNSUPPORTED;
+    };
+    (void)t0;
+    a = FastArgs{};
+    if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && esz == 8) ||
+        cfg.lx * cfg.ly * cfg.lz != 32 || cfg.kaxis > 2 || cfg.wx * cfg.wy * cfg.wz != 8)
+        return no("tile preset not available for this row type");
+    const uint32_t lane[3] = {cfg.lx, cfg.ly, cfg.lz}, warp[3] = {cfg.wx, cfg.wy, cfg.wz};
+    for (int k = 0; k < 3; k++) {
+        a.n[k] = vol.n[k];
+        a.lane[k] = lane[k];
+        a.warp[k] = warp[k];
+        a.tdim[k] = cfg.tile(k);
+        a.tiles[k] = (vol.n[k] + a.tdim[k] - 1) / a.tdim[k];
+    }
+    a.kax = cfg.kaxis;
+    a.oax0 = cfg.kaxis == 0 ? 1 : 0;
+    a.oax1 = cfg.kaxis == 2 ? 1 : 2;
+    const double sb = (confocal ? 2.0 : 1.0) / dT, sa = confocal ? 0.0 : 1.0 / dT;
+    a.sb = (float)sb;
+    a.sa = (float)sa;
+    for (int k = 0; k < 3; k++) {
+        a.h[k] = (float)hd[k];
+        a.hs[k] = (float)(hd[k] * sb);
+    }
+    a.L = L;
+    a.S = S;
+    a.T = T;
+    a.out_scale = 1.0f;
+    a.nvox = vol.count();
+    a.spin_limit = 1u << 22;
+    // Window width: the spread of (laser leg + SPAD leg) over a tile is at most
+    // (sa + sb) * tile diagonal (triangle inequality), plus margins and alignment.
+    double diag2 = 0.0;
+    for (int k = 0; k < 3; k++) {
+        const double e = (double)(a.tdim[k] - 1) * hd[k];
+        diag2 += e * e;
+    }
+    const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
+    a.align = 16 / esz;
+    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
+    const uint32_t bw_align = 128 / esz;
+    a.nbox = (w_need + 255) / 256;
+    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
+    if (a.BW > 256) return no("window box too wide");
+    a.W = a.BW * a.nbox;
+    a.row_bytes = a.W * esz;
+    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
+    uint32_t chunk = (uint32_t)std::min<uint64_t>(
+        std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, kMaxChunk), S);
+    uint32_t stages = std::min<uint32_t>(stages_req ? stages_req : cfg.stages, 8);
+    if (stages < 2) stages = 2;
+    // Shared memory per CTA so that the variant's resident-CTA target fits one SM (228 KB).
+    const int ctas = fast_ctas_per_sm((int)cfg.k, kahan, (int)esz);
+    const uint32_t soft = ctas >= 3 ? 72 * 1024 : (ctas == 2 ? 110 * 1024 : 200 * 1024);
+    const uint32_t budget = 200 * 1024;
+    if (!chunk_req)
+        while (chunk > 4 && stages * stage_bytes(chunk) > soft) chunk = (chunk + 1) / 2;
+    if (!stages_req)
+        while (stages > 2 && stages * stage_bytes(chunk) > soft) stages--;
+    while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
+    if (stages * stage_bytes(chunk) > budget)
+        return no("time window of one tile does not fit in shared memory (" +
+                  std::to_string(a.W) + " bins)");
+    a.chunk = chunk;
+    a.stages = stages;
+    a.stage_bytes = stage_bytes(chunk);
+    a.nchunks = (uint32_t)((S + chunk - 1) / chunk);
+    return BPGB_OK;
+}
+
+uint32_t fast_threads(const FastConfig &cfg) { return 32 * (1 + cfg.wx * cfg.wy * cfg.wz); }
+uint32_t fast_smem(const FastArgs &a) { return a.stages * a.stage_bytes + 128; }
 
 }  // namespace
 
@@ -563,29 +812,8 @@ struct FastPlan {
     float *d_partial = nullptr;
     uint64_t scratch = 0;
     int geom = 0;
+    uint32_t k = 8;
 };
-
-namespace {
-
-template <typename HT, int K>
-void *kernel_ptr(bool kahan, bool checked) {
-    if (kahan)
-        return checked ? (void *)bp_fast_kernel<HT, K, true, true>
-                       : (void *)bp_fast_kernel<HT, K, true, false>;
-    return checked ? (void *)bp_fast_kernel<HT, K, false, true>
-                   : (void *)bp_fast_kernel<HT, K, false, false>;
-}
-
-void *select_kernel(int dtype, bool kahan, bool checked) {
-    switch (dtype) {
-        case BPGB_DTYPE_F16: return kernel_ptr<__half, 8>(kahan, checked);
-        case BPGB_DTYPE_BF16: return kernel_ptr<__nv_bfloat16, 8>(kahan, checked);
-        case BPGB_DTYPE_C64: return kernel_ptr<float2, 8>(kahan, checked);
-        default: return kernel_ptr<float, 8>(kahan, checked);
-    }
-}
-
-}  // namespace
 
 int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
                     uint64_t P, const Factorization &fz, const Volume &vol,
@@ -612,66 +840,16 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     if (!(bp.dT > 0.0f)) return no("deltaT must be positive");
 
     const FastConfig cfg = fast_preset(opt.tile, dt);
-    FastArgs a{};
-    for (int k = 0; k < 3; k++) a.n[k] = vol.n[k];
-    a.lane[0] = cfg.lx;
-    a.lane[1] = cfg.ly;
-    a.lane[2] = cfg.lz;
-    a.warp[0] = cfg.wx;
-    a.warp[1] = cfg.wy;
-    a.warp[2] = cfg.wz;
-    if (cfg.k != 8 || cfg.lx * cfg.ly * cfg.lz != 32) return no("bad tile preset");
-    for (int k = 0; k < 3; k++) {
-        a.tdim[k] = cfg.tile(k);
-        a.tiles[k] = (vol.n[k] + a.tdim[k] - 1) / a.tdim[k];
-    }
     const bool confocal = fz.geom == GEOM_CONFOCAL;
-    const double dT = bp.dT;
-    const double sb = (confocal ? 2.0 : 1.0) / dT, sa = confocal ? 0.0 : 1.0 / dT;
-    a.sb = (float)sb;
-    a.sa = (float)sa;
-    for (int k = 0; k < 3; k++) {
-        a.h[k] = (float)hd[k];
-        a.hs[k] = (float)(hd[k] * sb);
-    }
-    a.L = confocal ? 1 : fz.L;
-    a.S = fz.S;
-    a.T = bp.T;
+    const uint64_t L = confocal ? 1 : fz.L;
+    FastArgs a;
+    std::string why;
+    int st = fast_args(a, cfg, vol, hd, confocal, bp.dT, bp.t0, L, fz.S, bp.T, esz,
+                       opt.accum == BPGB_ACCUM_KAHAN, opt.chunk > 0 ? (uint32_t)opt.chunk : 0,
+                       opt.stages > 0 ? (uint32_t)opt.stages : 0, &why);
+    if (st) return no(why);
     a.out_scale = opt.h_scale != 0.0f ? opt.h_scale : 1.0f;
-    a.nvox = vol.count();
-    a.spin_limit = opt.spin_limit ? opt.spin_limit : (1u << 22);
-
-    // Window width: the spread of (laser leg + SPAD leg) over a tile is at most
-    // (sa + sb) * tile diagonal (triangle inequality), plus margins and alignment.
-    double diag2 = 0.0;
-    for (int k = 0; k < 3; k++) {
-        const double e = (double)(a.tdim[k] - 1) * hd[k];
-        diag2 += e * e;
-    }
-    const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
-    a.align = 16 / esz;
-    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
-    const uint32_t bw_align = 128 / esz;
-    a.nbox = (w_need + 255) / 256;
-    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
-    if (a.BW > 256) return no("window box too wide");
-    a.W = a.BW * a.nbox;
-    a.row_bytes = a.W * esz;
-
-    // Stage sizing: keep all stages within ~200 KB of shared memory.
-    const uint32_t budget = 200 * 1024;
-    uint32_t chunk = std::min<uint64_t>(std::min<uint32_t>(cfg.chunk, kMaxChunk), fz.S);
-    uint32_t stages = std::min<uint32_t>(cfg.stages, 8);
-    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
-    while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
-    while (stages > 2 && stages * stage_bytes(chunk) > budget) stages--;
-    if (stages * stage_bytes(chunk) > budget)
-        return no("time window of one tile does not fit in shared memory (" +
-                  std::to_string(a.W) + " bins)");
-    a.chunk = chunk;
-    a.stages = stages;
-    a.stage_bytes = stage_bytes(chunk);
-    a.nchunks = (uint32_t)((fz.S + chunk - 1) / chunk);
+    if (opt.spin_limit) a.spin_limit = opt.spin_limit;
 
     auto *fp = new FastPlan();
     fp->dtype = dt;
@@ -680,10 +858,11 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     fp->P = P;
     fp->pitch = pitch;
     fp->geom = fz.geom;
-    fp->threads = 32 * (1 + cfg.wx * cfg.wy * cfg.wz);
-    fp->smem = a.stages * a.stage_bytes + 128;
+    fp->threads = fast_threads(cfg);
+    fp->smem = fast_smem(a);
 
-    void *kern = select_kernel(dt, fp->kahan, fp->checked);
+    fp->k = cfg.k;
+    void *kern = select_kernel(dt, fp->kahan, fp->checked, fp->k);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)fp->smem);
     if (e != cudaSuccess) {
@@ -716,6 +895,7 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
 
     // Device tables: SPAD entries (frame position relative to zero, row constant) and
     // laser entries (frame position, lw/dT - t0/dT), built in double on the host.
+    const double dT = bp.dT;
     std::vector<float4> tab(fz.S + a.L);
     auto frame = [&](const float *pt, double o[3]) {
         double d[3];
@@ -760,23 +940,14 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
 
 int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t stream) {
     const FastArgs &a = fp->a;
-    const uint32_t esz = dtype_bytes(fp->dtype);
     if (((uintptr_t)d_H) % 16) return set_error(BPGB_ERR_INVALID_ARGUMENT, "H must be 16-byte aligned");
     CUtensorMap map;
-    const cuuint64_t dims[2] = {a.T, fp->P};
-    const cuuint64_t strides[1] = {(cuuint64_t)fp->pitch * esz};
-    const cuuint32_t box[2] = {a.BW, 1};
-    const cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode_fn()(&map, tma_type(fp->dtype), 2, const_cast<void *>(d_H), dims, strides,
-                             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS)
-        return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    int st = encode_rows(&map, fp->dtype, d_H, a.T, fp->P, fp->pitch, a.BW);
+    if (st) return st;
     void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
-    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked);
+    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k);
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&fp->a};
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
@@ -1038,62 +1209,14 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
 
     // Launch arguments: the default tile preset of the FAST kernel, FP32 rows.
     const FastConfig cfg = fast_preset(-1, BPGB_DTYPE_F32);
-    FastArgs a{};
-    for (int k = 0; k < 3; k++) a.n[k] = vol.n[k];
-    a.lane[0] = cfg.lx;
-    a.lane[1] = cfg.ly;
-    a.lane[2] = cfg.lz;
-    a.warp[0] = cfg.wx;
-    a.warp[1] = cfg.wy;
-    a.warp[2] = cfg.wz;
-    for (int k = 0; k < 3; k++) {
-        a.tdim[k] = cfg.tile(k);
-        a.tiles[k] = (vol.n[k] + a.tdim[k] - 1) / a.tdim[k];
-    }
-    const double dT = deltaT;
-    const double sb = (confocal ? 2.0 : 1.0) / dT, sa = confocal ? 0.0 : 1.0 / dT;
-    a.sb = (float)sb;
-    a.sa = (float)sa;
-    for (int k = 0; k < 3; k++) {
-        a.h[k] = (float)hd[k];
-        a.hs[k] = (float)(hd[k] * sb);
-    }
-    a.L = num_lasers;
-    a.S = num_spads;
-    a.T = T;
-    a.out_scale = 1.0f;
-    a.nvox = vol.count();
-    a.spin_limit = 1u << 22;
-    double diag2 = 0.0;
-    for (int k = 0; k < 3; k++) {
-        const double e = (double)(a.tdim[k] - 1) * hd[k];
-        diag2 += e * e;
-    }
-    const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
-    const uint32_t esz = 4;
-    a.align = 16 / esz;
-    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
-    const uint32_t bw_align = 128 / esz;
-    a.nbox = (w_need + 255) / 256;
-    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
-    if (a.BW > 256) return set_error(BPGB_ERR_UNSUPPORTED, "window box too wide");
-    a.W = a.BW * a.nbox;
-    a.row_bytes = a.W * esz;
-    const uint32_t budget = 200 * 1024;
-    uint32_t chunk = (uint32_t)std::min<uint64_t>(std::min<uint32_t>(cfg.chunk, kMaxChunk), num_spads);
-    uint32_t stages = std::min<uint32_t>(cfg.stages, 8);
-    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
-    while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
-    while (stages > 2 && stages * stage_bytes(chunk) > budget) stages--;
-    if (stages * stage_bytes(chunk) > budget)
-        return set_error(BPGB_ERR_UNSUPPORTED, "time window of one tile does not fit in shared memory");
-    a.chunk = chunk;
-    a.stages = stages;
-    a.stage_bytes = stage_bytes(chunk);
-    a.nchunks = (uint32_t)((num_spads + chunk - 1) / chunk);
-    const uint32_t threads = 32 * (1 + cfg.wx * cfg.wy * cfg.wz);
-    const uint32_t smem = a.stages * a.stage_bytes + 128;
-    void *kern = select_kernel(BPGB_DTYPE_F32, false, false);
+    FastArgs a;
+    std::string why;
+    st = fast_args(a, cfg, vol, hd, confocal != 0, deltaT, t0, num_lasers, num_spads, T, 4, false,
+                   0, 0, &why);
+    if (st) return set_error(st, why);
+    const uint32_t threads = fast_threads(cfg);
+    const uint32_t smem = fast_smem(a);
+    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k);
     BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     BPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)threads, smem));
@@ -1121,7 +1244,7 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     for (int r = 0; r < 3; r++)
         for (int k = 0; k < 3; k++) ta.u[r][k] = u[r][k];
     for (int k = 0; k < 3; k++) ta.zero[k] = (double)vol.zero[k];
-    ta.dT = dT;
+    ta.dT = (double)deltaT;
     ta.t0 = (double)t0;
     ta.L = num_lasers;
     ta.S = num_spads;
@@ -1141,15 +1264,8 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
                          std::to_string(h[2]) + " pairs break the stated lasers x SPADs order");
 
     CUtensorMap map;
-    const cuuint64_t dims[2] = {T, P};
-    const cuuint64_t strides[1] = {(cuuint64_t)pitch * esz};
-    const cuuint32_t box[2] = {a.BW, 1};
-    const cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode_fn()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(d_H), dims,
-                             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    st = encode_rows(&map, BPGB_DTYPE_F32, d_H, T, P, pitch, a.BW);
+    if (st) return st;
     void *target = a.splits > 1 ? (void *)partial : (void *)d_volume;
     const float4 *spads = tab;
     const float4 *lasers = tab + num_spads;

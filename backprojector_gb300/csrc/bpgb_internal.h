@@ -65,12 +65,15 @@ bool volume_frame(const Volume &vol, double u[3][3], double h[3]);
 
 // ---- fast kernels (bp_fast.cu) ------------------------------------------------
 struct FastConfig {
-    // lane layout inside a warp (product 32), voxels per thread along z (K), warp layout
-    uint32_t lx, ly, lz, k, wx, wy, wz;
+    // lane layout inside a warp (product 32), voxels per thread (k) on a line along
+    // axis `kaxis`, consumer warp layout
+    uint32_t lx, ly, lz, k, wx, wy, wz, kaxis;
     uint32_t chunk;   // SPAD rows per pipeline stage (<= 32)
     uint32_t stages;  // pipeline depth
     uint32_t tile(int a) const {
-        return a == 0 ? lx * wx : (a == 1 ? ly * wy : lz * k * wz);
+        const uint32_t l = a == 0 ? lx : (a == 1 ? ly : lz);
+        const uint32_t w = a == 0 ? wx : (a == 1 ? wy : wz);
+        return l * w * ((uint32_t)a == kaxis ? k : 1);
     }
     uint32_t consumer_warps() const { return wx * wy * wz; }
 };

@@ -161,7 +161,8 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    cap = synthetic.make_capture(args.workload, seed=args.seed + rank)
+    over = {"voxels": args.voxels} if args.voxels else {}
+    cap = synthetic.make_capture(args.workload, seed=args.seed + rank, **over)
     phasor = args.workload == "phasor_128"
     N = tuple(int(v) for v in cap.voxels_per_side)
     stream = torch.cuda.Stream(device=dev)
@@ -261,16 +262,36 @@ def run_ours(args):
     clocks = clk.summary()
     sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    peak_updates = sms * MUFU_PER_SM_PER_CLK * sm_mhz * 1e6
+    # Pipe work of one FAST update: FP32 lanes (dz, q, x, +row constant, +1.5*2^23,
+    # accumulate; complex accumulates two lanes), one rsqrt, one shared gather (two bank
+    # slots for complex).  Pipe rates are measured on this GPU (bpgb_diag_pipe_rates).
+    try:
+        rates = capi.pipe_rates()
+        rate_src = "measured on this GPU by bpgb_diag_pipe_rates"
+    except Exception:
+        rates = {"rsqrt_per_sm_clk": float(MUFU_PER_SM_PER_CLK), "fp32_lanes_per_sm_clk": 128.0,
+                 "lds_per_sm_clk": 32.0}
+        rate_src = "nominal (probe unavailable)"
+    work = {"fp32": 7.0 if phasor else 6.0, "sfu": 1.0, "smem": 2.0 if phasor else 1.0}
+    per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / work["fp32"],
+               "sfu": rates["rsqrt_per_sm_clk"] / work["sfu"],
+               "smem": rates["lds_per_sm_clk"] / work["smem"]}
+    bound = min(per_clk, key=per_clk.get)
+    peak_updates = sms * per_clk[bound] * sm_mhz * 1e6
     achieved = updates / (ms * 1e-3)
     esz = {"f32": 4, "f16": 2}[args.dtype] if not phasor else 8
     algo_bytes = cap.P * cap.T * esz + cap.nvox * (8 if phasor else 4)
     roofline = {
-        "bound": "sfu", "kernel": "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel",
+        "bound": bound, "kernel": "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel",
         "achieved": achieved, "peak": peak_updates, "unit": "voxel-pair updates/s",
         "frac": achieved / peak_updates,
-        "peak_basis": f"{sms} SMs x {MUFU_PER_SM_PER_CLK} rsqrt/clk x {sm_mhz:.0f} MHz "
-                      "(median SM clock sampled during the timed region); one rsqrt per update",
+        "peak_basis": f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock in the timed region) x "
+                      f"min over pipes of rate / work per update: fp32 "
+                      f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:.0f}, sfu "
+                      f"{rates['rsqrt_per_sm_clk']:.1f} rsqrt/clk / {work['sfu']:.0f}, smem "
+                      f"{rates['lds_per_sm_clk']:.1f} loads/clk / {work['smem']:.0f}; rates "
+                      f"{rate_src}",
+        "pipe_rates_per_sm_clk": rates,
         "traffic": None,
         "algorithmic_bytes": algo_bytes,
         "hbm_achieved_gbs": algo_bytes / (ms * 1e-3) / 1e9,
@@ -342,6 +363,8 @@ def main():
     ap.add_argument("--kahan", action="store_true")
     ap.add_argument("--tile", type=int, default=None)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--voxels", type=int, default=None,
+                    help="override the volume resolution (reduced profiling cases)")
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--ref-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -86,7 +86,9 @@ typedef struct bpgb_options {
     int32_t pair_splits; /* CTAs sharing one voxel tile over disjoint pair ranges (0 = auto) */
     int32_t checked;     /* 1 = clamp and count out-of-window bins (tests) */
     uint32_t spin_limit; /* bounded mbarrier waits: polls before giving up (0 = default) */
-    int32_t reserved[7];
+    int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..32 (0 = from the preset) */
+    int32_t stages;      /* FAST: pipeline depth, 2..8 (0 = from the preset) */
+    int32_t reserved[5];
 } bpgb_options;
 
 /* Read-only description of a plan, for tests, the bench and the autotuner. */
@@ -197,6 +199,11 @@ int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h_pitch,
  * mbarrier that nothing arrives on.  Returns BPGB_ERR_TIMEOUT once `spin_limit` polls ran
  * out (the device stays usable), so callers and tests can check the timeout path. */
 int bpgb_diag_wait_timeout(uint32_t spin_limit);
+
+/* Measured per-SM, per-clock throughput on the current device of: rates[0] rsqrt.approx
+ * results (XU pipe), rates[1] FP32 lanes of packed FP32x2 FMAs, rates[2] conflict-free
+ * 32-bit shared-memory loads.  The roofline of the FAST update is derived from these. */
+int bpgb_diag_pipe_rates(double *rates);
 
 /* ---- phasor pulse --------------------------------------------------------
  * d_out[r, t] = sum_k d_H[r, t + k - K/2] * (cos_k, sin_k), read index in (0, T), with
