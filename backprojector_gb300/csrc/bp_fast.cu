@@ -66,6 +66,7 @@ struct FastArgs {
     uint32_t lane[3];   // lane layout (product 32)
     uint32_t warp[3];   // consumer warp layout
     uint32_t kax;       // axis of each thread's voxel line
+    uint32_t planar;    // every SPAD has the same frame coordinate along kax
     uint32_t oax0, oax1;  // the two other axes
     float h[3];         // voxel step length along each frame axis (m)
     float hs[3];        // h * sb (bins)
@@ -174,9 +175,11 @@ __device__ __forceinline__ float row_d(float v0, float v1, float e0, float e1) {
 
 // Window index (as float bits of x + 1.5*2^23) of one voxel; the scalar form of the
 // packed consumer arithmetic, used by the bin dump.
-__device__ __forceinline__ uint32_t window_bits(float vk, float D, float A, float ek, float ew) {
+__device__ __forceinline__ uint32_t window_bits(float vk, float D, float A, float ek, float ew,
+                                                bool planar) {
     const float dz = __fadd_rn(vk, -ek);
-    const float q = __fmaf_rn(dz, dz, D);
+    // planar walls: dz^2 is per voxel, formed once, then one add per row
+    const float q = planar ? __fadd_rn(D, __fmul_rn(dz, dz)) : __fmaf_rn(dz, dz, D);
     const float r = rsqrt_approx(q);
     const float y = __fmaf_rn(q, r, __fadd_rn(A, ew));
     return __float_as_uint(__fadd_rn(y, kMagic));
@@ -292,7 +295,7 @@ __host__ __device__ constexpr int fast_ctas_per_sm(int k, bool kahan, int esz) {
     return (void)kahan, (void)esz, k == 16 ? 1 : 2;
 }
 
-template <typename HT, int K, bool KAHAN, bool CHECKED>
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
 __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
     bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
                    const float4 *__restrict__ lasers, void *__restrict__ out,
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
                 lo = row_record(a, g, G, Lt, e, ew);
                 const float ek = sel3(e[0], e[1], e[2], a.kax);
                 table[2 * lane] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
-                                              sel3(e[0], e[1], e[2], a.oax1), 0.0f, 0.0f);
+                                              sel3(e[0], e[1], e[2], a.oax1), ew, ew);
                 table[2 * lane + 1] = make_float4(-ek, -ek, ew, ew);
             }
             __syncwarp();
@@ -416,6 +419,22 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     for (int i = 0; i < NP; i++) {
         vk[i].x = rel_coord(a, g, a.kax, bk + (2 * i) * kstep);
         vk[i].y = rel_coord(a, g, a.kax, bk + (2 * i + 1) * kstep);
+    }
+    // Planar wall: every row has the same kax coordinate (row_record's arithmetic on the
+    // first SPAD), so (v_k - c_k)^2 is formed once per voxel.
+    float2 dzsq[PLANAR ? NP : 1];
+    if (PLANAR) {
+        const float4 G0 = spads[0];
+        const float ek = __fmul_rn(sel3(G0.x, G0.y, G0.z, a.kax) -
+                                       __fmul_rn(sel3(g.ctr[0], g.ctr[1], g.ctr[2], a.kax),
+                                                 sel3(a.h[0], a.h[1], a.h[2], a.kax)),
+                                   a.sb);
+        const float2 nk = make_float2(-ek, -ek);
+#pragma unroll
+        for (int i = 0; i < (PLANAR ? NP : 1); i++) {
+            const float2 dz = __fadd2_rn(vk[i], nk);
+            dzsq[i] = __fmul2_rn(dz, dz);
+        }
     }
 
     PairT acc[NP], comp[NP];
@@ -478,19 +497,27 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
         // (one for complex rows, whose accumulators already double the registers).
 #pragma unroll(PairT::kEsz == 8 ? 1 : 2)
         for (uint32_t j = 0; j < nrows; j++) {
-            const float4 r0 = table[2 * j];
-            const float4 r1 = table[2 * j + 1];
+            const float4 r0 = table[2 * j];  // (c_o0, c_o1, ew, ew)
             const float D = row_d(v0, v1, r0.x, r0.y);
             const float2 D2 = make_float2(D, D);
-            const float2 nk = make_float2(r1.x, r1.y);
-            const float2 ew = make_float2(r1.z, r1.w);
+            const float2 ew = make_float2(r0.z, r0.w);
+            float2 nk = make_float2(0.0f, 0.0f);
+            if (!PLANAR) {
+                const float4 r1 = table[2 * j + 1];  // (-c_k, -c_k, ew, ew)
+                nk = make_float2(r1.x, r1.y);
+            }
             const uint32_t rbase = data + j * a.row_bytes - kMagicBits * esz;
 #pragma unroll
             for (int p = 0; p < NP; p++) {
                 // laser leg + row constant ahead of the rsqrt: one dependent op after it
                 const float2 Ae = __fadd2_rn(A[p], ew);
-                const float2 dz = __fadd2_rn(vk[p], nk);
-                const float2 q = __ffma2_rn(dz, dz, D2);
+                float2 q;
+                if (PLANAR) {
+                    q = __fadd2_rn(D2, dzsq[p]);
+                } else {
+                    const float2 dz = __fadd2_rn(vk[p], nk);
+                    q = __ffma2_rn(dz, dz, D2);
+                }
                 const float2 r = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
                 const float2 y = __ffma2_rn(q, r, Ae);
                 const float2 z = __fadd2_rn(y, magic2);
@@ -591,7 +618,7 @@ __global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
         const float vk = rel_coord(a, g, a.kax, sel3(idx[0], idx[1], idx[2], a.kax));
         const float D = row_d(v0, v1, sel3(e[0], e[1], e[2], a.oax0), sel3(e[0], e[1], e[2], a.oax1));
         const float ek = sel3(e[0], e[1], e[2], a.kax);
-        const int32_t rel = (int32_t)(window_bits(vk, D, A, ek, ew) - kMagicBits);
+        const int32_t rel = (int32_t)(window_bits(vk, D, A, ek, ew, a.planar != 0) - kMagicBits);
         const int32_t b = lo + rel;
         bins[w] = (b >= 0 && b < (int32_t)a.T) ? b : -1;
     }
@@ -681,28 +708,33 @@ const FastConfig kPresets[] = {
     {4, 1, 8, 16, 2, 1, 4, 1, 32, 4}, // 8 x 16 x 32, 4 x 8 lane blocks
 };
 
-template <typename HT, int K>
+template <typename HT, int K, bool PLANAR>
 void *kernel_ptr(bool kahan, bool checked) {
     if (kahan)
-        return checked ? (void *)bp_fast_kernel<HT, K, true, true>
-                       : (void *)bp_fast_kernel<HT, K, true, false>;
-    return checked ? (void *)bp_fast_kernel<HT, K, false, true>
-                   : (void *)bp_fast_kernel<HT, K, false, false>;
+        return checked ? (void *)bp_fast_kernel<HT, K, true, true, PLANAR>
+                       : (void *)bp_fast_kernel<HT, K, true, false, PLANAR>;
+    return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR>
+                   : (void *)bp_fast_kernel<HT, K, false, false, PLANAR>;
 }
 
-// K = 16 (twice the independent chains per thread) is built for the real row types;
-// complex rows keep K = 8 (twice the accumulator registers).
-void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k) {
-    const bool k16 = k == 16;
+template <typename HT>
+void *kernel_ptr8(bool kahan, bool checked, bool planar) {
+    return planar ? kernel_ptr<HT, 8, true>(kahan, checked) : kernel_ptr<HT, 8, false>(kahan, checked);
+}
+
+// Variants built: K = 8 for every row type, accumulation, check mode and wall shape;
+// K = 16 (one CTA per SM, 16 chains per thread) for FP32 rows with plain sums.
+void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar) {
+    if (k == 16) {
+        if (dtype != BPGB_DTYPE_F32 || kahan) return nullptr;
+        return checked ? (void *)bp_fast_kernel<float, 16, false, true, false>
+                       : (void *)bp_fast_kernel<float, 16, false, false, false>;
+    }
     switch (dtype) {
-        case BPGB_DTYPE_F16:
-            return k16 ? kernel_ptr<__half, 16>(kahan, checked) : kernel_ptr<__half, 8>(kahan, checked);
-        case BPGB_DTYPE_BF16:
-            return k16 ? kernel_ptr<__nv_bfloat16, 16>(kahan, checked)
-                       : kernel_ptr<__nv_bfloat16, 8>(kahan, checked);
-        case BPGB_DTYPE_C64: return kernel_ptr<float2, 8>(kahan, checked);
-        default:
-            return k16 ? kernel_ptr<float, 16>(kahan, checked) : kernel_ptr<float, 8>(kahan, checked);
+        case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar);
+        case BPGB_DTYPE_BF16: return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar);
+        case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar);
+        default: return kernel_ptr8<float>(kahan, checked, planar);
     }
 }
 
@@ -719,7 +751,7 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     };
     (void)t0;
     a = FastArgs{};
-    if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && esz == 8) ||
+    if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && (esz != 4 || kahan)) ||
         cfg.lx * cfg.ly * cfg.lz != 32 || cfg.kaxis > 2 || cfg.wx * cfg.wy * cfg.wz != 8)
         return no("tile preset not available for this row type");
     const uint32_t lane[3] = {cfg.lx, cfg.ly, cfg.lz}, warp[3] = {cfg.wx, cfg.wy, cfg.wz};
@@ -813,6 +845,7 @@ struct FastPlan {
     uint64_t scratch = 0;
     int geom = 0;
     uint32_t k = 8;
+    bool planar = false;
 };
 
 int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
@@ -862,7 +895,28 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     fp->smem = fast_smem(a);
 
     fp->k = cfg.k;
-    void *kern = select_kernel(dt, fp->kahan, fp->checked, fp->k);
+    // Planar wall: every SPAD's frame coordinate along the voxel-line axis is the same
+    // float (the table below computes the same value per SPAD).
+    bool planar = cfg.k == 8;
+    {
+        const double *uk = u[cfg.kaxis];
+        float first = 0.0f;
+        for (uint64_t s = 0; s < fz.S && planar; s++) {
+            const float *pt = h_pairs[s].camera_point;
+            double d[3];
+            for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
+            const float gk = (float)(uk[0] * d[0] + uk[1] * d[1] + uk[2] * d[2]);
+            if (s == 0) first = gk;
+            planar = std::memcmp(&gk, &first, sizeof(float)) == 0;
+        }
+    }
+    a.planar = planar ? 1 : 0;
+    fp->planar = planar;
+    void *kern = select_kernel(dt, fp->kahan, fp->checked, fp->k, fp->planar);
+    if (!kern) {
+        delete fp;
+        return no("tile preset not built for this row type / accumulation");
+    }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)fp->smem);
     if (e != cudaSuccess) {
@@ -947,7 +1001,7 @@ int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t s
     void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
-    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k);
+    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&fp->a};
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
@@ -1068,6 +1122,7 @@ struct NoAllocTableArgs {
     double dT, t0;
     uint64_t L, S;
     int confocal;
+    uint32_t kax;  // voxel-line axis of the tile preset (planar-wall test)
 };
 
 __device__ __forceinline__ void frame_fp64(const NoAllocTableArgs &t, const float *pt, double o[3]) {
@@ -1119,6 +1174,12 @@ __global__ void noalloc_tables_kernel(const bpgb_pair *__restrict__ pairs, const
                                   ? __ddiv_rn(__dadd_rn((double)pr.camera_wall, (double)pr.laser_wall), t.dT)
                                   : __ddiv_rn((double)pr.camera_wall, t.dT);
             tab[s] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)cs);
+            // planar wall: the same FP32 frame coordinate along kax as SPAD 0 (diag[4]
+            // counts SPADs off that plane)
+            double g0[3];
+            frame_fp64(t, pairs[0].camera_point, g0);
+            if (__float_as_uint((float)g[t.kax]) != __float_as_uint((float)g0[t.kax]))
+                atomicAdd(&diag[4], 1ull);
         }
         if (s == 0) {
             double g[3] = {0.0, 0.0, 0.0};
@@ -1216,7 +1277,7 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     if (st) return set_error(st, why);
     const uint32_t threads = fast_threads(cfg);
     const uint32_t smem = fast_smem(a);
-    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k);
+    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, false);  // general form first
     BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     BPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)threads, smem));
@@ -1249,19 +1310,27 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     ta.L = num_lasers;
     ta.S = num_spads;
     ta.confocal = confocal ? 1 : 0;
+    ta.kax = cfg.kaxis;
     const unsigned tblocks = (unsigned)std::min<uint64_t>((P + 255) / 256, 152ull * 16);
     noalloc_tables_kernel<<<tblocks, 256, 0, s>>>(d_pairs, ta, tab, diag);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     // A pair list with non-finite values or another order never reaches the window
     // arithmetic of the main kernel.
-    unsigned long long h[4] = {0, 0, 0, 0};
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
     BPGB_CUDA_TRY(cudaMemcpyAsync(h, diag, sizeof(h), cudaMemcpyDeviceToHost, s));
     BPGB_CUDA_TRY(cudaStreamSynchronize(s));
     if (h[3]) return set_error(BPGB_ERR_INVALID_ARGUMENT, std::to_string(h[3]) + " non-finite pair values");
     if (h[2])
         return set_error(BPGB_ERR_INVALID_ARGUMENT,
                          std::to_string(h[2]) + " pairs break the stated lasers x SPADs order");
+    // Same kernel variant as a plan on these pairs: the planar-wall form when every SPAD
+    // lies on one plane across the voxel lines.
+    if (h[4] == 0 && cfg.k == 8) {
+        a.planar = 1;
+        kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, true);
+        BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
 
     CUtensorMap map;
     st = encode_rows(&map, BPGB_DTYPE_F32, d_H, T, P, pitch, a.BW);

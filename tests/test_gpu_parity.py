@@ -223,6 +223,20 @@ def test_fast_complex_vs_oracle(cuda):
     assert oracle.rel_l2(out, ref) < 5e-3
 
 
+def test_fast_non_planar_wall_vs_oracle(cuda):
+    """SPADs off the wall plane (depth jitter): the general (non-planar) FAST arithmetic."""
+    c = _cap("precision_64", {}, seed=9)
+    pairs = c.pairs.copy()
+    jitter = np.random.default_rng(3).uniform(-0.02, 0.02, len(pairs)).astype(np.float32)
+    pairs["camera_point"][:, 1] += jitter
+    ref = oracle.bp_gpu_f64(c.H, pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    for checked in (1, 0):
+        out, info, viol = run_plan(cuda, c.H, pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                                   c.deltaT, algo=capi.ALGO_FAST, checked=checked)
+        assert info["algo"] == "fast" and viol == 0
+        assert oracle.rel_l2(out, ref) < 5e-3
+
+
 def test_confocal_fast_vs_oracle(cuda):
     c = synthetic.make_capture("precision_64", seed=7, small=True, confocal=True)
     ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
