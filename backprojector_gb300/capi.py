@@ -56,6 +56,23 @@ class PlanInfo(C.Structure):
         return d
 
 
+class CaptureGeometry(C.Structure):
+    _fields_ = [("pairs", C.c_void_p), ("num_pairs", C.c_uint64), ("T", C.c_uint32),
+                ("voxels_per_side", C.c_uint32 * 3), ("volume_zero_pos", C.c_float * 3),
+                ("voxel_inc", C.c_float * 9), ("t0", C.c_float), ("deltaT", C.c_float),
+                ("h_scale", C.c_float)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("captures", C.c_uint32), ("pitch", C.c_uint32), ("total_rows", C.c_uint64),
+                ("total_voxels", C.c_uint64), ("work_units", C.c_uint32), ("grid", C.c_uint32),
+                ("stages", C.c_uint32), ("chunk", C.c_uint32), ("smem_bytes", C.c_uint32),
+                ("updates", C.c_uint64), ("planar", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BackprojectorError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(message)
@@ -108,6 +125,14 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_synth_render": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_float, C.c_float, _F, _F,
                                     C.c_uint64, _F]),
     "bpgb_synth_poisson": (C.c_int, [_F, C.c_uint64, C.c_float, C.c_uint64]),
+    "bpgb_batch_create": (C.c_int, [C.POINTER(_P), C.POINTER(CaptureGeometry), C.c_uint32,
+                                    C.POINTER(Options)]),
+    "bpgb_batch_layout": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "bpgb_batch_get_info": (C.c_int, [_P, C.POINTER(BatchInfo)]),
+    "bpgb_batch_execute": (C.c_int, [_P, _P, _P, _P]),
+    "bpgb_batch_graph_launch": (C.c_int, [_P, _P, _P, _P]),
+    "bpgb_batch_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    "bpgb_batch_destroy": (C.c_int, [_P]),
 }
 
 _lib = None
@@ -352,3 +377,74 @@ def phasor_pulse_device(d_H, rows: int, T: int, in_pitch: int, wavelength: float
                         d_out, out_pitch: int, times: int = 4, stream=None) -> None:
     check(lib().bpgb_phasor_pulse(_ptr(d_H), rows, T, in_pitch, wavelength, deltaT, times,
                                   _ptr(d_out), out_pitch, _stream_ptr(stream)), "bpgb_phasor_pulse")
+
+
+class Batch:
+    """bpgb_batch: many captures (list of dicts or Capture-like objects with pairs, T,
+    voxels_per_side, zero, inc, t0, deltaT and optional h_scale) in one persistent launch.
+
+    Device buffers: H packed [total_rows, pitch] (capture c at rows row_offsets[c], bins
+    >= its T zero) and volumes packed [total_voxels] (capture c at voxel_offsets[c])."""
+
+    def __init__(self, captures, **opt):
+        self._pairs = [np.ascontiguousarray(c["pairs"], dtype=PAIR_DTYPE) for c in captures]
+        geo = (CaptureGeometry * len(captures))()
+        for i, c in enumerate(captures):
+            g = geo[i]
+            g.pairs = self._pairs[i].ctypes.data
+            g.num_pairs = len(self._pairs[i])
+            g.T = int(c["T"])
+            for k in range(3):
+                g.voxels_per_side[k] = int(c["voxels_per_side"][k])
+                g.volume_zero_pos[k] = float(c["zero"][k])
+            for k in range(9):
+                g.voxel_inc[k] = float(c["inc"][k])
+            g.t0 = float(c["t0"])
+            g.deltaT = float(c["deltaT"])
+            g.h_scale = float(c.get("h_scale", 1.0))
+        self.opt = options(**opt)
+        h = C.c_void_p()
+        check(lib().bpgb_batch_create(C.byref(h), geo, len(captures), C.byref(self.opt)),
+              "bpgb_batch_create")
+        self.handle = h
+        self.n = len(captures)
+        rows = (C.c_uint64 * self.n)()
+        vox = (C.c_uint64 * self.n)()
+        check(lib().bpgb_batch_layout(h, rows, vox), "bpgb_batch_layout")
+        self.row_offsets = [int(v) for v in rows]
+        self.voxel_offsets = [int(v) for v in vox]
+
+    def info(self) -> dict:
+        i = BatchInfo()
+        check(lib().bpgb_batch_get_info(self.handle, C.byref(i)), "bpgb_batch_get_info")
+        return i.as_dict()
+
+    def execute(self, d_H, d_volumes, stream=None) -> None:
+        check(lib().bpgb_batch_execute(self.handle, _ptr(d_H), _ptr(d_volumes), _stream_ptr(stream)),
+              "bpgb_batch_execute")
+
+    def graph_launch(self, d_H, d_volumes, stream=None) -> None:
+        check(lib().bpgb_batch_graph_launch(self.handle, _ptr(d_H), _ptr(d_volumes),
+                                            _stream_ptr(stream)), "bpgb_batch_graph_launch")
+
+    def check(self) -> int:
+        v = C.c_uint64()
+        check(lib().bpgb_batch_check(self.handle, C.byref(v)), "bpgb_batch_check")
+        return int(v.value)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bpgb_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -295,51 +295,51 @@ __host__ __device__ constexpr int fast_ctas_per_sm(int k, bool kahan, int esz) {
     return (void)kahan, (void)esz, k == 16 ? 1 : 2;
 }
 
+// Shared-memory state of a CTA's pipeline: stage ring, its mbarriers, the abort flag.
+struct PipeShared {
+    unsigned char *smem_raw;    // dynamic shared memory base
+    unsigned char *stage_base;  // 128-byte aligned stage ring
+    uint32_t pad;               // stage_base - smem_raw
+    uint64_t *full_bar, *empty_bar;
+    int *abort_flag;
+};
+
+// One work unit -- a voxel tile and a range of (laser, SPAD-chunk) items -- through the
+// producer / consumer pipeline.  `step` is the CTA's running pipeline step (stage =
+// step % stages, phase = step / stages); consecutive units of a persistent CTA continue
+// it, so the stage ring and its barriers carry over.  Rows of H are read at
+// row_base + l * S + s (the capture's first row in a packed buffer).  Returns false when
+// a bounded wait gave up (the CTA must stop).
 template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
-__global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
-    bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
-                   const float4 *__restrict__ lasers, void *__restrict__ out,
-                   unsigned long long *__restrict__ diag, const FastArgs a) {
+__device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *tmap,
+                                          const float4 *__restrict__ spads,
+                                          const float4 *__restrict__ lasers, void *out,
+                                          unsigned long long *diag, uint32_t tile,
+                                          uint32_t split, uint32_t row_base, uint64_t &step,
+                                          const PipeShared &sh) {
     using PairT = Pair<HT>;
     constexpr uint32_t esz = PairT::kEsz;
     constexpr int NP = K / 2;
-
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t full_bar[8];
-    __shared__ __align__(8) uint64_t empty_bar[8];
-    __shared__ int abort_flag;
-
-    // 128-byte aligned stage area
-    const uint32_t raw_addr = smem_addr(smem_raw);
-    const uint32_t pad = (128u - (raw_addr & 127u)) & 127u;
-    unsigned char *stage_base = smem_raw + pad;
+    unsigned char *const smem_raw = sh.smem_raw;
+    unsigned char *const stage_base = sh.stage_base;
+    const uint32_t pad = sh.pad;
+    uint64_t *const full_bar = sh.full_bar;
+    uint64_t *const empty_bar = sh.empty_bar;
+    int &abort_flag = *sh.abort_flag;
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t n_cons = a.warp[0] * a.warp[1] * a.warp[2];
-    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
-    const uint32_t tile = (uint32_t)(blockIdx.x % ntiles);
-    const uint32_t split = (uint32_t)(blockIdx.x / ntiles);
     const uint64_t items = a.L * a.nchunks;
     const uint64_t i0 = items * split / a.splits, i1 = items * (split + 1) / a.splits;
+    const uint64_t step0 = step;
+    step += i1 - i0;
 
     TileGeo g;
     tile_of_block(a, tile, g);
 
-    if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < a.stages; s++) {
-            mbar_init(smem_addr(&full_bar[s]), 1);
-            mbar_init(smem_addr(&empty_bar[s]), n_cons);
-        }
-        abort_flag = 0;
-        mbar_fence_init();
-    }
-    __syncthreads();
-
     if (warp == 0) {
         // ---------------- producer ----------------
-        uint64_t issued = 0;
         for (uint64_t it = i0; it < i1; it++) {
-            const uint64_t i = it - i0;
+            const uint64_t i = step0 + (it - i0);
             const uint32_t stage = (uint32_t)(i % a.stages);
             const uint32_t round = (uint32_t)(i / a.stages);
             if (round > 0) {
@@ -352,10 +352,14 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
                         atomicAdd(&diag[0], 1ull);
                         *(volatile int *)&abort_flag = 1;
                     }
-                    break;
+                    step = i;
+                    return false;
                 }
             }
-            if (*(volatile int *)&abort_flag) break;
+            if (*(volatile int *)&abort_flag) {
+                step = i;
+                return false;
+            }
             const uint64_t l = it / a.nchunks;
             const uint64_t s0 = (it % a.nchunks) * a.chunk;
             const uint32_t nrows =
@@ -379,28 +383,16 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
             if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
             __syncwarp();
             if (lane < nrows) {
-                const int32_t row = (int32_t)(l * a.S + s0 + lane);
+                const int32_t row = (int32_t)(row_base + l * a.S + s0 + lane);
                 const uint32_t dst = data + lane * a.row_bytes;
                 for (uint32_t b = 0; b < a.nbox; b++)
-                    tma_load_2d(dst + b * a.BW * esz, &tmap, lo + (int32_t)(b * a.BW), row, fb);
+                    tma_load_2d(dst + b * a.BW * esz, tmap, lo + (int32_t)(b * a.BW), row, fb);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(fb);
-            issued = i + 1;
         }
-        // Drain: every stage this CTA filled must have landed before the CTA may exit.
-        if (lane == 0) {
-            const uint64_t first = issued > a.stages ? issued - a.stages : 0;
-            for (uint64_t i = first; i < issued; i++) {
-                const uint32_t stage = (uint32_t)(i % a.stages);
-                if (!mbar_wait(smem_addr(&full_bar[stage]), (uint32_t)(i / a.stages) & 1,
-                               a.spin_limit))
-                    atomicAdd(&diag[0], 1ull);
-            }
-        }
-        return;
+        return true;
     }
-
     // ---------------- consumers ----------------
     const uint32_t cw = warp - 1;
     const uint32_t li[3] = {lane % a.lane[0], (lane / a.lane[0]) % a.lane[1],
@@ -449,7 +441,7 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     const uint32_t row_elems = a.row_bytes / esz;
 
     for (uint64_t it = i0; it < i1; it++) {
-        const uint64_t i = it - i0;
+        const uint64_t i = step0 + (it - i0);
         const uint32_t stage = (uint32_t)(i % a.stages);
         const uint32_t round = (uint32_t)(i / a.stages);
         const uint64_t l = it / a.nchunks;
@@ -479,7 +471,7 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
                 atomicAdd(&diag[0], 1ull);
                 *(volatile int *)&abort_flag = 1;
             }
-            break;
+            return false;
         }
         const uint64_t s0 = (it % a.nchunks) * a.chunk;
         const uint32_t nrows =
@@ -567,6 +559,54 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
                 acc[p].store(out, part_off + ((uint64_t)x * a.n[1] + y) * a.n[2] + z, w, scale);
         }
     }
+    return true;
+}
+
+// Producer lane 0 before the CTA exits: every stage the CTA filled must have landed
+// (bounded waits; the last `stages` steps are the only ones that can be in flight).
+__device__ __forceinline__ void pipeline_drain(uint32_t stages, uint64_t issued,
+                                               uint64_t *full_bar, unsigned long long *diag,
+                                               uint32_t spin_limit) {
+    if (threadIdx.x != 0) return;
+    const uint64_t first = issued > stages ? issued - stages : 0;
+    for (uint64_t i = first; i < issued; i++) {
+        const uint32_t stage = (uint32_t)(i % stages);
+        if (!mbar_wait(smem_addr(&full_bar[stage]), (uint32_t)(i / stages) & 1, spin_limit))
+            atomicAdd(&diag[0], 1ull);
+    }
+}
+
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
+__global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
+    bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
+                   const float4 *__restrict__ lasers, void *__restrict__ out,
+                   unsigned long long *__restrict__ diag, const FastArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[8];
+    __shared__ __align__(8) uint64_t empty_bar[8];
+    __shared__ int abort_flag;
+    PipeShared sh;
+    sh.smem_raw = smem_raw;
+    sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;  // 128-byte aligned stage ring
+    sh.stage_base = smem_raw + sh.pad;
+    sh.full_bar = full_bar;
+    sh.empty_bar = empty_bar;
+    sh.abort_flag = &abort_flag;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < a.stages; s++) {
+            mbar_init(smem_addr(&full_bar[s]), 1);
+            mbar_init(smem_addr(&empty_bar[s]), blockDim.x / 32 - 1);
+        }
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    uint64_t step = 0;
+    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, out, diag,
+                                             (uint32_t)(blockIdx.x % ntiles),
+                                             (uint32_t)(blockIdx.x / ntiles), 0, step, sh);
+    pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
 // out[v] = scale * sum_s partial[s][v], in split order (optionally Kahan).
@@ -744,7 +784,7 @@ void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar
 int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const double hd[3],
               bool confocal, double dT, double t0, uint64_t L, uint64_t S, uint32_t T,
               uint32_t esz, bool kahan, uint32_t chunk_req, uint32_t stages_req,
-              std::string *why) {
+              std::string *why, uint32_t bw_fixed = 0) {
     auto no = [&](const std::string &m) {
         if (why) *why = m;
         return BPGB_ERR_UNSUPPORTED;
@@ -789,8 +829,13 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     a.align = 16 / esz;
     const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
     const uint32_t bw_align = 128 / esz;
-    a.nbox = (w_need + 255) / 256;
-    a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
+    if (bw_fixed) {  // one TMA box width shared by several captures (batches)
+        a.BW = bw_fixed;
+        a.nbox = (w_need + bw_fixed - 1) / bw_fixed;
+    } else {
+        a.nbox = (w_need + 255) / 256;
+        a.BW = ((w_need + a.nbox - 1) / a.nbox + bw_align - 1) / bw_align * bw_align;
+    }
     if (a.BW > 256) return no("window box too wide");
     a.W = a.BW * a.nbox;
     a.row_bytes = a.W * esz;
@@ -917,14 +962,12 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
         delete fp;
         return no("tile preset not built for this row type / accumulation");
     }
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)fp->smem);
-    if (e != cudaSuccess) {
+    if (int rs = reserve_dynamic_smem(kern, fp->smem)) {
         delete fp;
-        return cuda_error(e, "cudaFuncSetAttribute(fast kernel)");
+        return rs;
     }
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)fp->threads, fp->smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)fp->threads, fp->smem);
     if (e != cudaSuccess || occ < 1) {
         delete fp;
         return e != cudaSuccess ? cuda_error(e, "occupancy query")
@@ -1090,6 +1133,435 @@ void fast_plan_free(FastPlan *fp) {
     if (fp->d_partial) cudaFree(fp->d_partial);
     delete fp;
 }
+
+// ==================================================================================
+// Batches: many captures of uneven grids, T and volumes in ONE persistent launch.
+//
+// All captures' rows live in one packed device buffer [sum P_c, pitch] (capture c at
+// rows row_base_c; bins T_c..pitch zero) behind a single TMA tensor map whose box width
+// is shared.  Each capture has a launch descriptor (FastArgs, table and output offsets)
+// in device memory.  The work list holds one (capture, tile) unit per voxel tile, sorted
+// by cost (pairs x tile voxels) in decreasing order; each CTA takes the next unit from
+// an atomic counter when it finishes one (greedy longest-first), with its pipeline (stage
+// ring, mbarrier phases) continuing across units.  The launch allocates nothing, so a caller can capture it in a CUDA graph;
+// bpgb_batch_graph_launch does that once per buffer pair and replays the graph.
+// ==================================================================================
+namespace {
+
+struct BatchCap {
+    FastArgs a;
+    uint64_t row_base;  // first row of the capture in the packed H
+    uint64_t out_off;   // first voxel of the capture in the packed output
+    uint64_t tab_off;   // first table entry (SPADs then lasers)
+};
+
+struct BatchUnit {
+    uint32_t cap, tile;
+};
+
+template <typename HT, bool CHECKED, bool PLANAR>
+__global__ void __launch_bounds__(288, 2)
+    bp_batch_kernel(const __grid_constant__ CUtensorMap tmap, const BatchCap *__restrict__ caps,
+                    const BatchUnit *__restrict__ units, uint32_t n_units,
+                    const float4 *__restrict__ tables, float *__restrict__ out,
+                    unsigned long long *__restrict__ diag, unsigned int *__restrict__ sched,
+                    uint32_t stages, uint32_t spin_limit) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[8];
+    __shared__ __align__(8) uint64_t empty_bar[8];
+    __shared__ int abort_flag;
+    PipeShared sh;
+    sh.smem_raw = smem_raw;
+    sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;
+    sh.stage_base = smem_raw + sh.pad;
+    sh.full_bar = full_bar;
+    sh.empty_bar = empty_bar;
+    sh.abort_flag = &abort_flag;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < stages; s++) {
+            mbar_init(smem_addr(&full_bar[s]), 1);
+            mbar_init(smem_addr(&empty_bar[s]), blockDim.x / 32 - 1);
+        }
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    // The unit's launch descriptor is staged in shared memory: fields are reloaded from
+    // there instead of held in registers (global loads would be hoisted and spill).
+    __shared__ __align__(16) BatchCap cap_s;
+    __shared__ uint32_t unit_s;
+    __syncthreads();
+    uint64_t step = 0;
+    bool ok = true;
+    for (;;) {
+        // Greedy longest-first: the next unit of the cost-sorted list goes to whichever
+        // CTA asks first (sched[0] counts handed-out units).
+        __syncthreads();  // every warp is done with the previous unit's descriptor
+        if (threadIdx.x == 0) unit_s = atomicAdd(&sched[0], 1u);
+        __syncthreads();
+        const uint32_t w = unit_s;
+        if (w >= n_units) break;
+        const BatchUnit u = units[w];
+        {
+            constexpr uint32_t kWords = sizeof(BatchCap) / 4;
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(caps + u.cap);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&cap_s);
+            for (uint32_t i = threadIdx.x; i < kWords; i += blockDim.x) dst[i] = src[i];
+        }
+        __syncthreads();
+        if (*(volatile int *)&abort_flag) break;
+        const float4 *tab = tables + cap_s.tab_off;
+        ok = fast_unit<HT, 8, false, CHECKED, PLANAR>(cap_s.a, &tmap, tab, tab + cap_s.a.S,
+                                                      out + cap_s.out_off, diag, u.tile, 0,
+                                                      (uint32_t)cap_s.row_base, step, sh);
+        if (!ok) *(volatile int *)&abort_flag = 1;
+    }
+    pipeline_drain(stages, step, full_bar, diag, spin_limit);
+    // The last CTA to finish re-arms the work counter for the next launch (graph replays).
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&sched[1], 1u) == gridDim.x - 1) {
+            atomicExch(&sched[0], 0u);
+            atomicExch(&sched[1], 0u);
+        }
+    }
+}
+
+void *select_batch_kernel(int dtype, bool checked, bool planar) {
+    if (dtype == BPGB_DTYPE_F16) {
+        if (planar) return checked ? (void *)bp_batch_kernel<__half, true, true> : (void *)bp_batch_kernel<__half, false, true>;
+        return checked ? (void *)bp_batch_kernel<__half, true, false> : (void *)bp_batch_kernel<__half, false, false>;
+    }
+    if (planar) return checked ? (void *)bp_batch_kernel<float, true, true> : (void *)bp_batch_kernel<float, false, true>;
+    return checked ? (void *)bp_batch_kernel<float, true, false> : (void *)bp_batch_kernel<float, false, false>;
+}
+
+}  // namespace
+
+struct BatchPlan {
+    int dtype = BPGB_DTYPE_F32;
+    bool checked = false, planar = false;
+    uint32_t n = 0, pitch = 0, stages = 0, chunk = 0, smem = 0, grid = 0, n_units = 0;
+    uint32_t spin_limit = 1u << 22;
+    uint64_t total_rows = 0, total_vox = 0, updates = 0;
+    std::vector<uint64_t> row_off, vox_off;
+    BatchCap *d_caps = nullptr;
+    BatchUnit *d_units = nullptr;
+    float4 *d_tables = nullptr;
+    unsigned long long *d_diag = nullptr;
+    unsigned int *d_sched = nullptr;  // work counter, finished-CTA counter
+    cudaStream_t own_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    const void *graph_H = nullptr;
+    const float *graph_out = nullptr;
+    cudaStream_t last_stream = nullptr;
+};
+
+void batch_free(BatchPlan *b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    cudaFree(b->d_caps);
+    cudaFree(b->d_units);
+    cudaFree(b->d_tables);
+    cudaFree(b->d_diag);
+    cudaFree(b->d_sched);
+    delete b;
+}
+
+int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
+    if (!d_H || !d_out) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null batch buffer");
+    if (((uintptr_t)d_H) % 16) return set_error(BPGB_ERR_INVALID_ARGUMENT, "H must be 16-byte aligned");
+    const uint32_t esz = dtype_bytes(b->dtype);
+    const cuuint64_t dims[2] = {b->pitch, b->total_rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)b->pitch * esz};
+    const cuuint32_t box[2] = {128 / esz, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUtensorMap map;
+    CUresult r = encode_fn()(&map, tma_type(b->dtype), 2, const_cast<void *>(d_H), dims, strides, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (batch)");
+    void *kern = select_batch_kernel(b->dtype, b->checked, b->planar);
+    void *args[] = {(void *)&map, (void *)&b->d_caps, (void *)&b->d_units, (void *)&b->n_units,
+                    (void *)&b->d_tables, (void *)&d_out, (void *)&b->d_diag, (void *)&b->d_sched,
+                    (void *)&b->stages, (void *)&b->spin_limit};
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(b->grid), dim3(288), args, b->smem, s));
+    count_launches(1);
+    b->last_stream = s;
+    return BPGB_OK;
+}
+
+}  // namespace bpgb
+
+using namespace bpgb;
+
+struct bpgb_batch_s : BatchPlan {};
+
+extern "C" {
+
+int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32_t n,
+                      const bpgb_options *opt) {
+    clear_error();
+    if (!out || (n && !caps)) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    if (n == 0) return set_error(BPGB_ERR_INVALID_ARGUMENT, "empty batch");
+    bpgb_options o;
+    bpgb_options_default(&o);
+    if (opt) o = *opt;
+    if (o.h_dtype != BPGB_DTYPE_F32 && o.h_dtype != BPGB_DTYPE_F16)
+        return set_error(BPGB_ERR_UNSUPPORTED, "batches take FP32 or FP16 rows");
+    if (o.accum != BPGB_ACCUM_F32)
+        return set_error(BPGB_ERR_UNSUPPORTED, "batches accumulate in FP32");
+    int sms = 0;
+    int st = require_device(&sms);
+    if (st) return st;
+    const uint32_t esz = dtype_bytes(o.h_dtype);
+    const uint32_t bw = 128 / esz;
+    FastConfig cfg = fast_preset(o.tile, o.h_dtype);
+    if (cfg.k != 8) cfg = fast_preset(0, o.h_dtype);
+    auto *b = new bpgb_batch_s();
+    b->n = n;
+    b->dtype = o.h_dtype;
+    b->checked = o.checked != 0;
+    if (o.spin_limit) b->spin_limit = o.spin_limit;
+    std::vector<BatchCap> hc(n);
+    std::vector<float4> tabs;
+    uint32_t max_row_bytes = 0, tmax = 0;
+    bool planar = true;
+    for (uint32_t c = 0; c < n; c++) {
+        const bpgb_capture_geometry &g = caps[c];
+        auto fail = [&](int code, const std::string &m) {
+            batch_free(b);
+            return set_error(code, "capture " + std::to_string(c) + ": " + m);
+        };
+        if (!g.pairs || g.num_pairs == 0 || g.T == 0) return fail(BPGB_ERR_INVALID_ARGUMENT, "empty capture");
+        Volume vol{};
+        for (int k = 0; k < 3; k++) {
+            vol.n[k] = g.voxels_per_side[k];
+            vol.zero[k] = g.volume_zero_pos[k];
+        }
+        for (int k = 0; k < 9; k++) vol.inc[k] = g.voxel_inc[k];
+        BinParams bp{g.t0, g.deltaT, g.T};
+        std::string why;
+        if (!finite_geometry(g.pairs, g.num_pairs, vol, bp, &why)) return fail(BPGB_ERR_INVALID_ARGUMENT, why);
+        const Factorization fz = factorize_pairs(g.pairs, g.num_pairs);
+        if (fz.geom != GEOM_SINGLE_LASER && fz.geom != GEOM_EXHAUSTIVE && fz.geom != GEOM_CONFOCAL)
+            return fail(BPGB_ERR_UNSUPPORTED, "pair list does not factor as lasers x SPADs");
+        double u[3][3], hd[3];
+        if (!volume_frame(vol, u, hd)) return fail(BPGB_ERR_UNSUPPORTED, "voxel basis is not orthogonal");
+        const bool confocal = fz.geom == GEOM_CONFOCAL;
+        const uint64_t L = confocal ? 1 : fz.L;
+        FastArgs &a = hc[c].a;
+        st = fast_args(a, cfg, vol, hd, confocal, g.deltaT, g.t0, L, fz.S, g.T, esz, false,
+                       o.chunk > 0 ? (uint32_t)o.chunk : 0, o.stages > 0 ? (uint32_t)o.stages : 0,
+                       &why, bw);
+        if (st) return fail(st, why);
+        a.out_scale = g.h_scale != 0.0f ? g.h_scale : 1.0f;
+        a.splits = 1;
+        a.spin_limit = b->spin_limit;
+        max_row_bytes = std::max(max_row_bytes, a.row_bytes);
+        tmax = std::max(tmax, g.T);
+        // tables (same FP64 arithmetic as a plan) and the planar-wall test
+        const double dT = g.deltaT;
+        auto frame = [&](const float *pt, double f[3]) {
+            double d[3];
+            for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
+            for (int r = 0; r < 3; r++) f[r] = u[r][0] * d[0] + u[r][1] * d[1] + u[r][2] * d[2];
+        };
+        hc[c].tab_off = tabs.size();
+        float first = 0.0f;
+        for (uint64_t s = 0; s < fz.S; s++) {
+            const bpgb_pair &pr = g.pairs[s];
+            double f[3];
+            frame(pr.camera_point, f);
+            const double cs = confocal ? ((double)pr.camera_wall + (double)pr.laser_wall) / dT
+                                       : (double)pr.camera_wall / dT;
+            tabs.push_back(make_float4((float)f[0], (float)f[1], (float)f[2], (float)cs));
+            const float gk = (float)f[cfg.kaxis];
+            if (s == 0) first = gk;
+            planar = planar && std::memcmp(&gk, &first, sizeof(float)) == 0;
+        }
+        for (uint64_t l = 0; l < L; l++) {
+            double f[3] = {0.0, 0.0, 0.0};
+            double cst = -(double)g.t0 / dT;
+            if (!confocal) {
+                const bpgb_pair &pr = g.pairs[l * fz.S];
+                frame(pr.laser_point, f);
+                cst += (double)pr.laser_wall / dT;
+            }
+            tabs.push_back(make_float4((float)f[0], (float)f[1], (float)f[2], (float)cst));
+        }
+        hc[c].row_base = b->total_rows;
+        hc[c].out_off = b->total_vox;
+        b->row_off.push_back(b->total_rows);
+        b->vox_off.push_back(b->total_vox);
+        b->total_rows += g.num_pairs;
+        b->total_vox += vol.count();
+        b->updates += vol.count() * g.num_pairs;
+    }
+    if (b->total_rows >= (1ull << 31)) {
+        batch_free(b);
+        return set_error(BPGB_ERR_UNSUPPORTED, "batch has too many rows for TMA coordinates");
+    }
+    // common stage ring: the widest window sets the row slot
+    uint32_t chunk = o.chunk > 0 ? std::min<uint32_t>((uint32_t)o.chunk, kMaxChunk) : cfg.chunk;
+    uint32_t stages = o.stages > 0 ? std::min<uint32_t>((uint32_t)o.stages, 8) : cfg.stages;
+    stages = std::max<uint32_t>(stages, 2);
+    auto stage_bytes = [&](uint32_t ch) { return kTableBytes + ch * max_row_bytes; };
+    while (chunk > 4 && stages * stage_bytes(chunk) > 110 * 1024) chunk = (chunk + 1) / 2;
+    while (stages > 2 && stages * stage_bytes(chunk) > 110 * 1024) stages--;
+    while (chunk > 1 && stages * stage_bytes(chunk) > 200 * 1024) chunk = (chunk + 1) / 2;
+    if (stages * stage_bytes(chunk) > 200 * 1024) {
+        batch_free(b);
+        return set_error(BPGB_ERR_UNSUPPORTED, "widest time window does not fit in shared memory");
+    }
+    b->chunk = chunk;
+    b->stages = stages;
+    b->smem = stages * stage_bytes(chunk) + 128;
+    b->planar = planar;
+    b->pitch = (tmax + bw - 1) / bw * bw;
+    std::vector<BatchUnit> units;
+    std::vector<uint64_t> cost;
+    for (uint32_t c = 0; c < n; c++) {
+        FastArgs &a = hc[c].a;
+        a.chunk = chunk;
+        a.stages = stages;
+        a.stage_bytes = stage_bytes(chunk);
+        a.nchunks = (uint32_t)((a.S + chunk - 1) / chunk);
+        a.planar = planar ? 1 : 0;
+        const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+        for (uint64_t t = 0; t < ntiles; t++) units.push_back({c, (uint32_t)t});
+    }
+    // longest units first (pairs x tile voxels), stable within a capture
+    std::vector<uint32_t> order(units.size());
+    for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
+    auto unit_cost = [&](const BatchUnit &u) {
+        const FastArgs &a = hc[u.cap].a;
+        return (uint64_t)a.L * a.S * a.tdim[0] * a.tdim[1] * a.tdim[2];
+    };
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t x, uint32_t y) { return unit_cost(units[x]) > unit_cost(units[y]); });
+    std::vector<BatchUnit> sorted(units.size());
+    for (size_t i = 0; i < order.size(); i++) sorted[i] = units[order[i]];
+    b->n_units = (uint32_t)sorted.size();
+    void *kern = select_batch_kernel(b->dtype, b->checked, b->planar);
+    if (int rs = reserve_dynamic_smem(kern, b->smem)) {
+        batch_free(b);
+        return rs;
+    }
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 288, b->smem);
+    if (e != cudaSuccess || occ < 1) {
+        batch_free(b);
+        return e != cudaSuccess ? cuda_error(e, "batch kernel attributes")
+                                : set_error(BPGB_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
+    }
+    b->grid = (uint32_t)std::min<uint64_t>(b->n_units, (uint64_t)sms * occ);
+    e = cudaMalloc(&b->d_caps, n * sizeof(BatchCap));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_units, sorted.size() * sizeof(BatchUnit));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_diag, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_caps, hc.data(), n * sizeof(BatchCap), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_units, sorted.data(), sorted.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_diag, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_sched, 0, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return cuda_error(e, "batch upload");
+    }
+    *out = b;
+    return BPGB_OK;
+}
+
+int bpgb_batch_layout(bpgb_batch b, uint64_t *row_offsets, uint64_t *voxel_offsets) {
+    if (!b) return set_error(BPGB_ERR_INVALID_ARGUMENT, "batch is null");
+    for (uint32_t c = 0; c < b->n; c++) {
+        if (row_offsets) row_offsets[c] = b->row_off[c];
+        if (voxel_offsets) voxel_offsets[c] = b->vox_off[c];
+    }
+    return BPGB_OK;
+}
+
+int bpgb_batch_get_info(bpgb_batch b, bpgb_batch_info *info) {
+    if (!b || !info) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->captures = b->n;
+    info->pitch = b->pitch;
+    info->total_rows = b->total_rows;
+    info->total_voxels = b->total_vox;
+    info->work_units = b->n_units;
+    info->grid = b->grid;
+    info->stages = b->stages;
+    info->chunk = b->chunk;
+    info->smem_bytes = b->smem;
+    info->updates = b->updates;
+    info->planar = b->planar ? 1 : 0;
+    return BPGB_OK;
+}
+
+int bpgb_batch_execute(bpgb_batch b, const void *d_H, float *d_volumes, void *stream) {
+    clear_error();
+    if (!b) return set_error(BPGB_ERR_INVALID_ARGUMENT, "batch is null");
+    return batch_execute(b, d_H, d_volumes, (cudaStream_t)stream);
+}
+
+int bpgb_batch_graph_launch(bpgb_batch b, const void *d_H, float *d_volumes, void *stream) {
+    clear_error();
+    if (!b) return set_error(BPGB_ERR_INVALID_ARGUMENT, "batch is null");
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->own_stream;
+    if (!b->graph || b->graph_H != d_H || b->graph_out != d_volumes) {
+        if (b->graph) {
+            cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+        }
+        cudaStream_t cap = b->own_stream;
+        BPGB_CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+        int st = batch_execute(b, d_H, d_volumes, cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cap, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_error(e, "batch graph capture");
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_error(e, "batch graph instantiate");
+        b->graph_H = d_H;
+        b->graph_out = d_volumes;
+    }
+    BPGB_CUDA_TRY(cudaGraphLaunch(b->graph, s));
+    b->last_stream = s;
+    return BPGB_OK;
+}
+
+int bpgb_batch_check(bpgb_batch b, uint64_t *violations) {
+    clear_error();
+    if (!b) return set_error(BPGB_ERR_INVALID_ARGUMENT, "batch is null");
+    BPGB_CUDA_TRY(cudaStreamSynchronize(b->last_stream));
+    unsigned long long h[2] = {0, 0};
+    BPGB_CUDA_TRY(cudaMemcpy(h, b->d_diag, sizeof(h), cudaMemcpyDeviceToHost));
+    BPGB_CUDA_TRY(cudaMemset(b->d_diag, 0, sizeof(h)));
+    if (violations) *violations = h[1];
+    if (h[0]) return set_error(BPGB_ERR_TIMEOUT, std::to_string(h[0]) + " device waits timed out");
+    if (h[1]) return set_error(BPGB_ERR_WINDOW, std::to_string(h[1]) + " bins fell outside their window");
+    return BPGB_OK;
+}
+
+int bpgb_batch_destroy(bpgb_batch b) {
+    batch_free(b);
+    return BPGB_OK;
+}
+
+}  // extern "C"
+
+namespace bpgb {
 
 }  // namespace bpgb
 
@@ -1278,7 +1750,8 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     const uint32_t threads = fast_threads(cfg);
     const uint32_t smem = fast_smem(a);
     void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, false);  // general form first
-    BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    st = reserve_dynamic_smem(kern, smem);
+    if (st) return st;
     int occ = 0;
     BPGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)threads, smem));
     if (occ < 1) return set_error(BPGB_ERR_UNSUPPORTED, "fast kernel does not fit on an SM");
@@ -1329,7 +1802,8 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     if (h[4] == 0 && cfg.k == 8) {
         a.planar = 1;
         kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, true);
-        BPGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        st = reserve_dynamic_smem(kern, smem);
+        if (st) return st;
     }
 
     CUtensorMap map;

@@ -27,6 +27,11 @@ void count_launches(uint64_t n);
 // Checks that a GB300-class device (compute capability 10.x) is current.
 int require_device(int *sm_count = nullptr);
 
+// Raises (never lowers) a kernel's dynamic shared memory limit on the current device to
+// at least `bytes`.  Plans and batches that share a kernel function stay launchable
+// whatever order they were created in.
+int reserve_dynamic_smem(const void *kernel, uint32_t bytes);
+
 // ---- volume description -------------------------------------------------------
 struct Volume {
     uint32_t n[3];
@@ -62,6 +67,11 @@ Factorization factorize_pairs(const bpgb_pair *pairs, uint64_t P);
 // Orthonormal frame of the voxel basis: rows u[0..2] and the step lengths h[0..2].
 // Returns false when the basis is not orthogonal (then only EXACT applies).
 bool volume_frame(const Volume &vol, double u[3][3], double h[3]);
+
+// Every pair value, the volume origin / steps, t0 and deltaT are finite (deltaT != 0);
+// otherwise *why names the first offender.
+bool finite_geometry(const bpgb_pair *pairs, uint64_t P, const Volume &vol,
+                     const BinParams &bp, std::string *why);
 
 // ---- fast kernels (bp_fast.cu) ------------------------------------------------
 struct FastConfig {

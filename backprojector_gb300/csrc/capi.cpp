@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -50,6 +51,21 @@ int require_device(int *sm_count) {
                          "this build targets sm_103a (GB300); device major version " +
                              std::to_string(major));
     if (sm_count) *sm_count = sms;
+    return BPGB_OK;
+}
+
+int reserve_dynamic_smem(const void *kernel, uint32_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, uint32_t> limits;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    uint32_t &cur = limits[{dev, kernel}];
+    if (bytes <= cur) return BPGB_OK;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(max dynamic shared memory)");
+    cur = bytes;
     return BPGB_OK;
 }
 
@@ -136,7 +152,7 @@ bool volume_frame(const Volume &vol, double u[3][3], double h[3]) {
     return true;
 }
 
-static bool finite_geometry(const bpgb_pair *pairs, uint64_t P, const Volume &vol,
+bool finite_geometry(const bpgb_pair *pairs, uint64_t P, const Volume &vol,
                             const BinParams &bp, std::string *why) {
     for (uint64_t p = 0; p < P; p++) {
         const float *f = reinterpret_cast<const float *>(&pairs[p]);

@@ -88,11 +88,9 @@ int launch_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in
         cudaFreeAsync(d_taps, stream);
         return set_error(BPGB_ERR_UNSUPPORTED, "phasor pulse too long for shared memory");
     }
-    e = cudaFuncSetAttribute(phasor_pulse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    if (e != cudaSuccess) {
+    if (int rs = reserve_dynamic_smem((const void *)phasor_pulse_kernel, (uint32_t)smem)) {
         cudaFreeAsync(d_taps, stream);
-        return cuda_error(e, "phasor smem attribute");
+        return rs;
     }
     const uint64_t blocks = rows * nseg;
     if (blocks >= (1ull << 31)) {

@@ -284,3 +284,61 @@ def make_capture(name: str, seed: int = 0, small: bool = False, render: bool = T
         wl = float(np.float32(spec.wavelength_spacings * spacing))
     return Capture(spec, seed, H, pairs, las_grid, cam_grid, lpos, cpos, t0, dT, vpos, vsize, n,
                    zero, inc, points, albedo, wl)
+
+
+# ---------------------------------------------------------------- batches
+
+BATCH_GRIDS = (16, 32, 48, 64, 96)
+BATCH_T = (512, 1024, 2048)
+BATCH_VOXELS = (32, 48, 64, 96)
+
+
+def make_batch(n: int = 64, seed: int = 0, render: bool = True, grids=BATCH_GRIDS,
+               Ts=BATCH_T, voxels=BATCH_VOXELS, exhaustive_frac: float = 0.25,
+               exhaustive_grid: int = 16) -> list[Capture]:
+    """Seeded uneven batch: n captures with SPAD grids g^2 (g from `grids`), T from `Ts`,
+    volumes v^3 (v from `voxels`) and 4-40 point scatterers each.
+
+    A fraction `exhaustive_frac` of the captures has a laser grid equal to its SPAD grid;
+    those take the `exhaustive_grid`^2 grid (16^2: 65,536 pairs, the dense exhaustive
+    shape), the others one
+    laser at the wall centre.  Wall 1 x 1 m, deltaT 3 mm, volume a 0.5 m cube 0.6 m behind
+    the wall (the dense configuration's geometry).  Capture i uses seed `seed * 1000 + i`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        exhaustive = bool(rng.random() < exhaustive_frac)
+        g = exhaustive_grid if exhaustive else int(rng.choice(grids))
+        T = int(rng.choice(Ts))
+        v = int(rng.choice(voxels))
+        k = int(rng.integers(4, 41))
+        out.append(make_capture(
+            "dense_exhaustive_16", seed=seed * 1000 + i, render=render,
+            laser_grid=(g, g) if exhaustive else None, spad_grid=(g, g), T=T, voxels=v,
+            scene_params={"n": k, "albedo": (0.2, 1.0)}))
+    return out
+
+
+def batch_geometry(caps: list[Capture], scales=None) -> list[dict]:
+    """Per-capture geometry dicts for capi.Batch (scales: per-capture H scale)."""
+    return [{"pairs": c.pairs, "T": c.T, "voxels_per_side": c.voxels_per_side, "zero": c.zero,
+             "inc": c.inc, "t0": c.t0, "deltaT": c.deltaT,
+             "h_scale": 1.0 if scales is None else float(scales[i])} for i, c in enumerate(caps)]
+
+
+def fp16_scales(caps: list[Capture]) -> np.ndarray:
+    """Per-capture scale s with H / s inside FP16 range (peak at 2^15)."""
+    return np.array([max(float(np.abs(c.H).max()), 1e-30) / 32768.0 for c in caps], np.float32)
+
+
+def pack_batch(caps: list[Capture], row_offsets, pitch: int, dtype=np.float16,
+               scales=None) -> np.ndarray:
+    """Packed H [total_rows, pitch]: capture c's rows at row_offsets[c], divided by its
+    scale and converted to `dtype`; bins beyond a capture's T are zero."""
+    total = int(row_offsets[-1]) + caps[-1].P
+    H = np.zeros((total, pitch), dtype)
+    for i, c in enumerate(caps):
+        r = int(row_offsets[i])
+        h = c.H if scales is None else c.H / np.float32(scales[i])
+        H[r:r + c.P, :c.T] = h.astype(dtype)
+    return H

@@ -34,6 +34,10 @@ WORKLOADS = {
     "precision_64": "dense, 1 laser x 64x64 SPADs, T=2048, dT=1mm, 64^3 over a 1 m cube",
     "dense_exhaustive_16": "dense, 16x16 lasers x 16x16 SPADs, T=512, dT=3mm, 32^3 over 0.5 m",
     "phasor_128": "phasor complex64, 1 laser x 128x128 SPADs, T=4096, dT=0.5mm, 128^3 over 1.5 m",
+    "batch_64": "64 uneven captures in one persistent launch replayed from a CUDA graph: SPAD "
+                "grids {16,32,48,64,96}^2 (1 laser, or 16^2 x 16^2 exhaustive for a quarter), "
+                "T {512,1024,2048}, volumes {32,48,64,96}^3, 4-40 scatterers, FP16 rows with a "
+                "per-capture scale, FP32 accumulate",
 }
 MUFU_PER_SM_PER_CLK = 16  # reciprocal square root throughput of one SM (Blackwell SFU)
 
@@ -123,6 +127,8 @@ def run_reference_arm(args):
         return
     from backprojector_gb300 import synthetic
 
+    if args.workload == "batch_64":
+        return run_reference_arm_batch(args)
     cap = synthetic.make_capture(args.workload, seed=args.seed)
     for _ in range(args.warmup):
         cpu_baseline(cap, args.ref_sample, seed=1)
@@ -143,6 +149,37 @@ def run_reference_arm(args):
         "cpu_baseline": {"value": value, "unit": "updates/s", "cores": cores, "kind": "port",
                          "sample": f"{args.ref_sample} voxels x {cap.P} pairs per step; "
                                    "classic_backprojection restated in C (OpenMP)"},
+        "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_arm_batch(args):
+    """--impl reference on batch_64: each step reconstructs a seeded voxel sample of every
+    capture of the batch with the reference's CPU path."""
+    from backprojector_gb300 import synthetic
+
+    caps = synthetic.make_batch(64, seed=args.seed)
+    per = max(1, args.ref_sample // 4)
+    for _ in range(args.warmup):
+        cpu_baseline_batch(caps, per, seed=1)
+    upd, secs, cores = 0.0, [], None
+    for k in range(args.steps):
+        r, dt, _, cores = cpu_baseline_batch(caps, per, seed=100 + k)
+        upd += r * dt
+        secs.append(dt)
+    value = float(upd / np.sum(secs))
+    sample = (f"{per} seeded random voxels of each of the 64 captures x all their pairs per "
+              "step; classic_backprojection restated in C (OpenMP)")
+    line = {
+        "impl": "reference", "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": float(np.mean(secs) * 1e3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batch_64: {WORKLOADS['batch_64']}", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "updates/s", "cores": cores, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -258,46 +295,11 @@ def run_ours(args):
                "ms_per_step": e2e_s * 1e3,
                "path": "bpgb_backproject_host (plan + H2D + kernel + D2H, synchronous)"}
 
-    peaks = measured_peaks()
     clocks = clk.summary()
-    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    sms = torch.cuda.get_device_properties(dev).multi_processor_count
-    # Pipe work of one FAST update: FP32 lanes (dz, q, x, +row constant, +1.5*2^23,
-    # accumulate; complex accumulates two lanes), one rsqrt, one shared gather (two bank
-    # slots for complex).  Pipe rates are measured on this GPU (bpgb_diag_pipe_rates).
-    try:
-        rates = capi.pipe_rates()
-        rate_src = "measured on this GPU by bpgb_diag_pipe_rates"
-    except Exception:
-        rates = {"rsqrt_per_sm_clk": float(MUFU_PER_SM_PER_CLK), "fp32_lanes_per_sm_clk": 128.0,
-                 "lds_per_sm_clk": 32.0}
-        rate_src = "nominal (probe unavailable)"
-    work = {"fp32": 7.0 if phasor else 6.0, "sfu": 1.0, "smem": 2.0 if phasor else 1.0}
-    per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / work["fp32"],
-               "sfu": rates["rsqrt_per_sm_clk"] / work["sfu"],
-               "smem": rates["lds_per_sm_clk"] / work["smem"]}
-    bound = min(per_clk, key=per_clk.get)
-    peak_updates = sms * per_clk[bound] * sm_mhz * 1e6
-    achieved = updates / (ms * 1e-3)
     esz = {"f32": 4, "f16": 2}[args.dtype] if not phasor else 8
     algo_bytes = cap.P * cap.T * esz + cap.nvox * (8 if phasor else 4)
-    roofline = {
-        "bound": bound, "kernel": "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel",
-        "achieved": achieved, "peak": peak_updates, "unit": "voxel-pair updates/s",
-        "frac": achieved / peak_updates,
-        "peak_basis": f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock in the timed region) x "
-                      f"min over pipes of rate / work per update: fp32 "
-                      f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:.0f}, sfu "
-                      f"{rates['rsqrt_per_sm_clk']:.1f} rsqrt/clk / {work['sfu']:.0f}, smem "
-                      f"{rates['lds_per_sm_clk']:.1f} loads/clk / {work['smem']:.0f}; rates "
-                      f"{rate_src}",
-        "pipe_rates_per_sm_clk": rates,
-        "traffic": None,
-        "algorithmic_bytes": algo_bytes,
-        "hbm_achieved_gbs": algo_bytes / (ms * 1e-3) / 1e9,
-        "hbm_peak_gbs": peaks.get("hbm_gbs"),
-        "hbm_frac": algo_bytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
-    }
+    roofline = roofline_for(updates / (ms * 1e-3), ms, algo_bytes, phasor, clocks, dev,
+                            "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel")
     tr = ROOT / "profiles" / f"traffic_{args.workload}.json"
     if tr.exists():
         try:
@@ -336,6 +338,205 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_batch(args):
+    """batch_64: every capture of the batch reconstructed per step by one graph replay of
+    the persistent batch kernel; e2e adds the packed FP16 rows' upload and the volumes'
+    download around it."""
+    import torch
+
+    from backprojector_gb300 import capi, synthetic
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    caps = synthetic.make_batch(64, seed=args.seed + rank)
+    scales = synthetic.fp16_scales(caps)
+    geo = synthetic.batch_geometry(caps, scales)
+    opt = dict(h_dtype=capi.DTYPE_F16)
+    if args.tile is not None:
+        opt["tile"] = args.tile
+    gate = capi.Batch(geo, checked=1, **opt)
+    info = gate.info()
+    Hh = synthetic.pack_batch(caps, gate.row_offsets, info["pitch"], np.float16, scales)
+    dH = torch.from_numpy(Hh).to(dev)
+    dV = torch.empty(info["total_voxels"], dtype=torch.float32, device=dev)
+    gate.execute(dH, dV)
+    if gate.check() != 0:
+        raise RuntimeError("window check failed: bins outside the staged windows")
+    gate.close()
+    batch = capi.Batch(geo, **opt)
+    info = batch.info()
+    stream = torch.cuda.Stream(device=dev)
+
+    def step():
+        batch.graph_launch(dH, dV, stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    batch.check()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = capi.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    # graph replays launch the captured kernel once each; the capture itself counted one
+    launches = max(capi.launch_count() - launches0, 0) + args.steps
+    ms = e0.elapsed_time(e1) / args.steps
+    batch.check()
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    updates = int(info["updates"])
+    value = updates * ws / (ms * 1e-3)
+
+    # the same captures one plan each, back to back (what a caller without batches does)
+    plans = []
+    for i, c in enumerate(caps):
+        r = batch.row_offsets[i]
+        plans.append((capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                                h_dtype=capi.DTYPE_F16, h_scale=float(scales[i]),
+                                h_pitch=info["pitch"]),
+                      dH[r:r + c.P], dV[batch.voxel_offsets[i]:batch.voxel_offsets[i] + c.nvox]))
+    hp = Hh  # keep numpy alive
+    for p, h, v in plans:
+        p.execute(h, v, stream)
+    stream.synchronize()
+    s0 = torch.cuda.Event(enable_timing=True)
+    s1 = torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for p, h, v in plans:
+        p.execute(h, v, stream)
+    s1.record(stream)
+    s1.synchronize()
+    per_plan_ms = s0.elapsed_time(s1)
+    for p, _, _ in plans:
+        p.close()
+
+    # e2e: pinned packed rows up, graph replay, volumes down, every step
+    hH = torch.from_numpy(hp).pin_memory()
+    hV = torch.empty(info["total_voxels"], dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            dH.copy_(hH, non_blocking=True)
+            batch.graph_launch(dH, dV, stream)
+            hV.copy_(dV, non_blocking=True)
+        stream.synchronize()
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t) / args.steps
+    e2e = {"value": updates * ws / e2e_s, "unit": "updates/s",
+           "h2d_bytes_per_step": int(hH.numel() * 2), "d2h_bytes_per_step": int(hV.numel() * 4),
+           "ms_per_step": e2e_s * 1e3,
+           "path": "capi.Batch.graph_launch with the packed rows copied up and the volumes "
+                   "copied down inside each step"}
+    clocks = clk.summary()
+    algo_bytes = int(sum(c.P * c.T * 2 + c.nvox * 4 for c in caps))
+    roofline = roofline_for(updates / (ms * 1e-3), ms, algo_bytes, False, clocks, dev,
+                            "bp_batch_kernel")
+    line = {
+        "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16 storage, f32 accumulate",
+        "data": "synthetic (seeded scenes rendered per pair; no dataset available)",
+        "config": {"workload": f"batch_64: {WORKLOADS['batch_64']}", "captures": len(caps),
+                   "updates_per_step": updates, "batch": info,
+                   "l2": f"inputs larger than L2 (packed H = {Hh.nbytes / 1e6:.0f} MB > 129 MB)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "roofline": roofline,
+        "per_capture_plans": {"ms_per_step": per_plan_ms,
+                              "value": updates / (per_plan_ms * 1e-3), "unit": "updates/s",
+                              "note": "the same 64 captures as 64 plan launches on one stream"},
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        r, dt, nvs, cores = cpu_baseline_batch(caps, max(1, args.cpu_sample // 64))
+        line["cpu_baseline"] = {"value": r, "unit": "updates/s", "cores": cores, "kind": "port",
+                                "sample": f"{nvs} seeded random voxels of each of the 64 "
+                                          f"captures x all their pairs ({dt:.1f} s); reference "
+                                          "classic_backprojection restated in C with OpenMP"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline_batch(caps, per_capture: int, seed: int = 0):
+    """cpu_baseline over every capture of a batch: `per_capture` voxels of each."""
+    upd, secs, cores = 0, 0.0, None
+    for i, c in enumerate(caps):
+        r, dt, n, cores = cpu_baseline(c, per_capture, seed=seed * 1000 + i)
+        upd += n * c.P
+        secs += dt
+    return upd / secs, secs, per_capture, cores
+
+
+def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel):
+    """Roofline of the FAST kernels: per-update pipe work against the pipe rates measured
+    on this GPU, at the median SM clock of the timed region."""
+    import torch
+
+    from backprojector_gb300 import capi
+
+    peaks = measured_peaks()
+    sm_mhz = clocks.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    # Pipe work of one FAST update: FP32 lanes (dz, q, x, +row constant, +1.5*2^23,
+    # accumulate; complex accumulates two lanes), one rsqrt, one shared gather (two bank
+    # slots for complex).  Pipe rates are measured on this GPU (bpgb_diag_pipe_rates).
+    try:
+        rates = capi.pipe_rates()
+        rate_src = "measured on this GPU by bpgb_diag_pipe_rates"
+    except Exception:
+        rates = {"rsqrt_per_sm_clk": float(MUFU_PER_SM_PER_CLK), "fp32_lanes_per_sm_clk": 128.0,
+                 "lds_per_sm_clk": 32.0}
+        rate_src = "nominal (probe unavailable)"
+    work = {"fp32": 7.0 if phasor else 6.0, "sfu": 1.0, "smem": 2.0 if phasor else 1.0}
+    per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / work["fp32"],
+               "sfu": rates["rsqrt_per_sm_clk"] / work["sfu"],
+               "smem": rates["lds_per_sm_clk"] / work["smem"]}
+    bound = min(per_clk, key=per_clk.get)
+    peak_updates = sms * per_clk[bound] * sm_mhz * 1e6
+    return {
+        "bound": bound, "kernel": kernel,
+        "achieved": achieved, "peak": peak_updates, "unit": "voxel-pair updates/s",
+        "frac": achieved / peak_updates,
+        "peak_basis": f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock in the timed region) x "
+                      f"min over pipes of rate / work per update: fp32 "
+                      f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:.0f}, sfu "
+                      f"{rates['rsqrt_per_sm_clk']:.1f} rsqrt/clk / {work['sfu']:.0f}, smem "
+                      f"{rates['lds_per_sm_clk']:.1f} loads/clk / {work['smem']:.0f}; rates "
+                      f"{rate_src}",
+        "pipe_rates_per_sm_clk": rates,
+        "traffic": None,
+        "algorithmic_bytes": algo_bytes,
+        "hbm_achieved_gbs": algo_bytes / (ms * 1e-3) / 1e9,
+        "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        "hbm_frac": algo_bytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+    }
+
+
 def reference_gpu(cap):
     """The reference's own kernel (built from its sources) on this GPU: one run."""
     try:
@@ -372,6 +573,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.workload == "batch_64":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -195,6 +195,55 @@ int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h_pitch,
                              const float *volume_zero_pos, const float *voxel_inc, float t0,
                              float deltaT, float *d_volume, void *stream);
 
+/* ---- batches: many captures in one persistent launch ---------------------------
+ * No counterpart in the reference (it reconstructs one capture per call and relaunches
+ * a 16^3 grid per 4096 voxels).  A batch holds the geometry of n captures of uneven pair
+ * grids, T and volumes.  Their rows are packed into ONE device buffer
+ * [total_rows, pitch] (capture c starts at row_offsets[c]; bins T_c..pitch-1 must be
+ * zero) of opt->h_dtype (FP32 or FP16; per-capture h_scale multiplies the result), and
+ * their volumes into one float buffer (capture c at voxel_offsets[c]).  execute runs
+ * every voxel tile of every capture in one persistent kernel, longest tiles first, each
+ * CTA taking the next tile from a device work counter that the launch re-arms when it
+ * ends; graph_launch captures that launch in a CUDA graph once per (d_H, d_volumes)
+ * pair and replays it.  Launches of ONE batch must not overlap (stream-order them):
+ * they share the work counter.  Each capture's pairs must factor as lasers x SPADs or
+ * be confocal. */
+typedef struct bpgb_capture_geometry {
+    const bpgb_pair *pairs; /* host pair list of the capture */
+    uint64_t num_pairs;
+    uint32_t T;
+    uint32_t voxels_per_side[3];
+    float volume_zero_pos[3];
+    float voxel_inc[9];
+    float t0, deltaT;
+    float h_scale; /* result multiplier for this capture (FP16 per-capture scale); 0 = 1 */
+} bpgb_capture_geometry;
+
+typedef struct bpgb_batch_info {
+    uint32_t captures;
+    uint32_t pitch;       /* elements per packed row */
+    uint64_t total_rows;  /* rows of the packed H */
+    uint64_t total_voxels;
+    uint32_t work_units;  /* voxel tiles over all captures */
+    uint32_t grid;        /* persistent CTAs */
+    uint32_t stages, chunk, smem_bytes;
+    uint64_t updates;     /* voxel x pair updates per execute */
+    int32_t planar;       /* the planar-wall kernel variant runs */
+} bpgb_batch_info;
+
+typedef struct bpgb_batch_s *bpgb_batch;
+
+int bpgb_batch_create(bpgb_batch *batch, const bpgb_capture_geometry *captures, uint32_t n,
+                      const bpgb_options *opt);
+/* row_offsets / voxel_offsets: n entries each (either may be NULL). */
+int bpgb_batch_layout(bpgb_batch batch, uint64_t *row_offsets, uint64_t *voxel_offsets);
+int bpgb_batch_get_info(bpgb_batch batch, bpgb_batch_info *info);
+int bpgb_batch_execute(bpgb_batch batch, const void *d_H, float *d_volumes, void *stream);
+int bpgb_batch_graph_launch(bpgb_batch batch, const void *d_H, float *d_volumes, void *stream);
+/* Synchronises and reports device diagnostics like bpgb_plan_check. */
+int bpgb_batch_check(bpgb_batch batch, uint64_t *violations);
+int bpgb_batch_destroy(bpgb_batch batch);
+
 /* Failure-path probe: a one-warp kernel waits, with the pipeline's bounded wait, on an
  * mbarrier that nothing arrives on.  Returns BPGB_ERR_TIMEOUT once `spin_limit` polls ran
  * out (the device stays usable), so callers and tests can check the timeout path. */

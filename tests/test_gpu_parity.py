@@ -259,6 +259,26 @@ def test_fast_pair_splits_deterministic(cuda, splits):
     assert oracle.rel_l2(a, ref) < 5e-3
 
 
+def test_plans_sharing_a_kernel_stay_launchable(cuda):
+    """Plans of one kernel variant with different shared memory footprints, created in
+    either order, all launch (the per-kernel limit is only ever raised)."""
+    import torch
+
+    caps = [_cap("precision_64", {}), _cap("octree_256", {}), _cap(*CASES[0])]
+    plans = [capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                       algo=capi.ALGO_FAST) for c in caps]
+    smem = [p.info()["smem_bytes"] for p in plans]
+    assert len(set(smem)) > 1, smem
+    for p, c in reversed(list(zip(plans, caps))):
+        dH = torch.from_numpy(c.H).to(cuda)
+        dV = torch.empty(tuple(int(v) for v in c.voxels_per_side), device=cuda)
+        p.execute(dH, dV)
+        p.check()
+        ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+        assert oracle.rel_l2(dV.cpu().numpy(), ref) < 5e-3
+        p.close()
+
+
 @pytest.mark.parametrize("tile", list(range(6)))
 def test_fast_tile_presets(cuda, tile):
     c = _cap("octree_256", {})
