@@ -73,6 +73,15 @@ class BatchInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_uint32), ("cache_hit", C.c_uint32), ("default_ms", C.c_float),
+                ("best_ms", C.c_float), ("tile", C.c_int32), ("chunk", C.c_int32),
+                ("stages", C.c_int32), ("pair_splits", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BackprojectorError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(message)
@@ -133,6 +142,14 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_batch_graph_launch": (C.c_int, [_P, _P, _P, _P]),
     "bpgb_batch_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "bpgb_batch_destroy": (C.c_int, [_P]),
+    "bpgb_plan_autotune": (C.c_int, [_P, C.c_uint64, C.c_uint32, _U32, _F, _F, C.c_float, C.c_float,
+                                     _P, _P, C.POINTER(Options), C.POINTER(TuneReport), _P]),
+    "bpgb_batch_autotune": (C.c_int, [C.POINTER(CaptureGeometry), C.c_uint32, _P, _P,
+                                      C.POINTER(Options), C.POINTER(TuneReport), _P]),
+    "bpgb_tune_cache_save": (C.c_int, [C.c_char_p]),
+    "bpgb_tune_cache_load": (C.c_int, [C.c_char_p]),
+    "bpgb_tune_cache_clear": (C.c_int, []),
+    "bpgb_tune_cache_size": (C.c_int, []),
 }
 
 _lib = None
@@ -387,21 +404,7 @@ class Batch:
     >= its T zero) and volumes packed [total_voxels] (capture c at voxel_offsets[c])."""
 
     def __init__(self, captures, **opt):
-        self._pairs = [np.ascontiguousarray(c["pairs"], dtype=PAIR_DTYPE) for c in captures]
-        geo = (CaptureGeometry * len(captures))()
-        for i, c in enumerate(captures):
-            g = geo[i]
-            g.pairs = self._pairs[i].ctypes.data
-            g.num_pairs = len(self._pairs[i])
-            g.T = int(c["T"])
-            for k in range(3):
-                g.voxels_per_side[k] = int(c["voxels_per_side"][k])
-                g.volume_zero_pos[k] = float(c["zero"][k])
-            for k in range(9):
-                g.voxel_inc[k] = float(c["inc"][k])
-            g.t0 = float(c["t0"])
-            g.deltaT = float(c["deltaT"])
-            g.h_scale = float(c.get("h_scale", 1.0))
+        geo, self._pairs = _capture_geometry_array(captures)
         self.opt = options(**opt)
         h = C.c_void_p()
         check(lib().bpgb_batch_create(C.byref(h), geo, len(captures), C.byref(self.opt)),
@@ -448,3 +451,71 @@ class Batch:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---------------------------------------------------------------- autotuner
+
+TUNED_KEYS = ("tile", "chunk", "stages", "pair_splits")
+
+
+def _capture_geometry_array(captures):
+    keep = [np.ascontiguousarray(c["pairs"], dtype=PAIR_DTYPE) for c in captures]
+    geo = (CaptureGeometry * len(captures))()
+    for i, c in enumerate(captures):
+        g = geo[i]
+        g.pairs = keep[i].ctypes.data
+        g.num_pairs = len(keep[i])
+        g.T = int(c["T"])
+        for k in range(3):
+            g.voxels_per_side[k] = int(c["voxels_per_side"][k])
+            g.volume_zero_pos[k] = float(c["zero"][k])
+        for k in range(9):
+            g.voxel_inc[k] = float(c["inc"][k])
+        g.t0 = float(c["t0"])
+        g.deltaT = float(c["deltaT"])
+        g.h_scale = float(c.get("h_scale", 1.0))
+    return geo, keep
+
+
+def autotune_plan(pairs, T, voxels_per_side, zero, inc, t0, deltaT, d_H, d_volume, stream=None,
+                  **opt) -> tuple[dict, dict]:
+    """bpgb_plan_autotune: returns (tuned option overrides, report).  d_H holds the
+    capture's rows (read), d_volume is overwritten."""
+    pr = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+    n = np.asarray([int(v) for v in voxels_per_side], np.uint32)
+    o = options(**opt)
+    rep = TuneReport()
+    check(lib().bpgb_plan_autotune(vptr(pr), len(pr), int(T), u32ptr(n), fptr(f32(zero)),
+                                   fptr(f32(inc)), t0, deltaT, _ptr(d_H), _ptr(d_volume),
+                                   C.byref(o), C.byref(rep), _stream_ptr(stream)),
+          "bpgb_plan_autotune")
+    tuned = {k: getattr(o, k) for k in TUNED_KEYS}
+    tuned["algo"] = o.algo
+    return tuned, rep.as_dict()
+
+
+def autotune_batch(captures, d_H, d_volumes, stream=None, **opt) -> tuple[dict, dict]:
+    """bpgb_batch_autotune over capture geometry dicts (as for Batch)."""
+    geo, keep = _capture_geometry_array(captures)
+    o = options(**opt)
+    rep = TuneReport()
+    check(lib().bpgb_batch_autotune(geo, len(captures), _ptr(d_H), _ptr(d_volumes), C.byref(o),
+                                    C.byref(rep), _stream_ptr(stream)), "bpgb_batch_autotune")
+    del keep
+    return {k: getattr(o, k) for k in TUNED_KEYS[:3]}, rep.as_dict()
+
+
+def tune_cache_save(path) -> None:
+    check(lib().bpgb_tune_cache_save(str(path).encode()), "bpgb_tune_cache_save")
+
+
+def tune_cache_load(path) -> None:
+    check(lib().bpgb_tune_cache_load(str(path).encode()), "bpgb_tune_cache_load")
+
+
+def tune_cache_clear() -> None:
+    lib().bpgb_tune_cache_clear()
+
+
+def tune_cache_size() -> int:
+    return int(lib().bpgb_tune_cache_size())

@@ -226,6 +226,13 @@ def run_ours(args):
             dH = (dH / scale).half()
             opt["h_scale"] = scale
         dV = torch.empty(N, dtype=torch.float32, device=dev)
+    tune_rep = None
+    if not args.no_tune and args.tile is None and args.algo == "fast":
+        t = time.perf_counter()
+        tuned, tune_rep = capi.autotune_plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0,
+                                             cap.deltaT, dH, dV, **opt)
+        tune_rep["seconds"] = time.perf_counter() - t
+        opt.update(tuned)
     # Gate: the bounds-checked kernel variant must see every bin inside its staged window
     # before the unchecked variant runs.
     with capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, checked=1,
@@ -317,7 +324,8 @@ def run_ours(args):
         "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload]}", "P": cap.P,
                    "T": cap.T, "voxels": list(N), "updates_per_step": updates,
                    "l2": f"inputs larger than L2 (H = {cap.H.nbytes / 1e6:.0f} MB > 129 MB)",
-                   "plan": info, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                   "plan": info, "autotune": tune_rep,
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "roofline": roofline,
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -359,11 +367,19 @@ def run_batch(args):
     opt = dict(h_dtype=capi.DTYPE_F16)
     if args.tile is not None:
         opt["tile"] = args.tile
-    gate = capi.Batch(geo, checked=1, **opt)
-    info = gate.info()
-    Hh = synthetic.pack_batch(caps, gate.row_offsets, info["pitch"], np.float16, scales)
+    layout = capi.Batch(geo, **opt)  # row / voxel layout does not depend on the tile shape
+    info = layout.info()
+    Hh = synthetic.pack_batch(caps, layout.row_offsets, info["pitch"], np.float16, scales)
+    layout.close()
     dH = torch.from_numpy(Hh).to(dev)
     dV = torch.empty(info["total_voxels"], dtype=torch.float32, device=dev)
+    tune_rep = None
+    if not args.no_tune and args.tile is None:
+        t = time.perf_counter()
+        tuned, tune_rep = capi.autotune_batch(geo, dH, dV, **opt)
+        tune_rep["seconds"] = time.perf_counter() - t
+        opt.update(tuned)
+    gate = capi.Batch(geo, checked=1, **opt)
     gate.execute(dH, dV)
     if gate.check() != 0:
         raise RuntimeError("window check failed: bins outside the staged windows")
@@ -458,7 +474,7 @@ def run_batch(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f16 storage, f32 accumulate",
         "data": "synthetic (seeded scenes rendered per pair; no dataset available)",
         "config": {"workload": f"batch_64: {WORKLOADS['batch_64']}", "captures": len(caps),
-                   "updates_per_step": updates, "batch": info,
+                   "updates_per_step": updates, "batch": info, "autotune": tune_rep,
                    "l2": f"inputs larger than L2 (packed H = {Hh.nbytes / 1e6:.0f} MB > 129 MB)",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "roofline": roofline,
@@ -562,7 +578,9 @@ def main():
     ap.add_argument("--algo", choices=["fast", "exact"], default="fast")
     ap.add_argument("--dtype", choices=["f32", "f16"], default="f32")
     ap.add_argument("--kahan", action="store_true")
-    ap.add_argument("--tile", type=int, default=None)
+    ap.add_argument("--tile", type=int, default=None,
+                    help="fixed tile preset (skips the autotuner)")
+    ap.add_argument("--no-tune", action="store_true", help="untuned default configuration")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--voxels", type=int, default=None,
                     help="override the volume resolution (reduced profiling cases)")

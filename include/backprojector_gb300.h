@@ -244,6 +244,40 @@ int bpgb_batch_graph_launch(bpgb_batch batch, const void *d_H, float *d_volumes,
 int bpgb_batch_check(bpgb_batch batch, uint64_t *violations);
 int bpgb_batch_destroy(bpgb_batch batch);
 
+/* ---- autotuner -------------------------------------------------------------------
+ * No counterpart in the reference (its launch shape is fixed: 16^3 voxels per launch,
+ * the largest power-of-two block not above the pair count).  Times FAST configurations
+ * on the caller's device buffers (contents are read, results are overwritten) on
+ * `stream`, in three stages: every tile preset at its own chunk and depth; chunk
+ * {8,16,32} x depth {2,3,4,6} on the two fastest presets; pair splits {1,2,4} on the
+ * winner (plans only).  The winner is re-run with bin-window checking; a candidate
+ * that puts any bin outside its window is never chosen.  On return opt->tile, chunk,
+ * stages and pair_splits hold the choice (and opt->algo = FAST for plans); the other
+ * fields of *opt (row type, accumulation, pitch, scale) are inputs.  Choices are cached
+ * per device and workload shape for the life of the process (a cache hit times
+ * nothing); bpgb_tune_cache_save / _load persist the cache as a text file. */
+typedef struct bpgb_tune_report {
+    uint32_t candidates; /* configurations timed (0 on a cache hit) */
+    uint32_t cache_hit;
+    float default_ms;    /* the untuned first preset at its own chunk/depth (-1: not run) */
+    float best_ms;       /* the choice, ms per execute */
+    int32_t tile, chunk, stages, pair_splits;
+} bpgb_tune_report;
+
+int bpgb_plan_autotune(const bpgb_pair *host_pairs, uint64_t num_pairs, uint32_t T,
+                       const uint32_t *voxels_per_side, const float *volume_zero_pos,
+                       const float *voxel_inc, float t0, float deltaT, const void *d_H,
+                       void *d_volume, bpgb_options *opt, bpgb_tune_report *report,
+                       void *stream);
+int bpgb_batch_autotune(const bpgb_capture_geometry *captures, uint32_t n, const void *d_H,
+                        float *d_volumes, bpgb_options *opt, bpgb_tune_report *report,
+                        void *stream);
+int bpgb_tune_cache_save(const char *path);
+/* Merges the file's entries into the cache; a missing file is not an error. */
+int bpgb_tune_cache_load(const char *path);
+int bpgb_tune_cache_clear(void);
+int bpgb_tune_cache_size(void);
+
 /* Failure-path probe: a one-warp kernel waits, with the pipeline's bounded wait, on an
  * mbarrier that nothing arrives on.  Returns BPGB_ERR_TIMEOUT once `spin_limit` polls ran
  * out (the device stays usable), so callers and tests can check the timeout path. */

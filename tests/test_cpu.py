@@ -169,3 +169,27 @@ def test_oracle_pinned_to_reference_kernel_outputs():
             assert oracle.rel_l2(emu[mask], ref[mask]) < 1e-4, f.name
         assert oracle.rel_l2(o64[mask], ref[mask]) < 2e-2, f.name
         assert np.all(ref[~mask] == 0), f.name
+
+
+def test_tune_cache_file_round_trip(tmp_path):
+    """The autotuner's cache file: load merges entries, save writes them back, bad lines
+    are rejected with the line number (no device needed)."""
+    capi.tune_cache_clear()
+    src = tmp_path / "tune.txt"
+    src.write_text("plan/GB300/sm152/dt0/acc0/P16384/T4096/n256x256x256 3 16 4 0 88.5\n"
+                   "batch/GB300/sm152/dt1/n64/shapeabc 1 32 3 0 140.25\n")
+    capi.tune_cache_load(src)
+    assert capi.tune_cache_size() == 2
+    out = tmp_path / "saved.txt"
+    capi.tune_cache_save(out)
+    lines = sorted(out.read_text().split("\n")[:-1])
+    assert lines == sorted(src.read_text().split("\n")[:-1])
+    capi.tune_cache_load(tmp_path / "missing.txt")  # no file yet: not an error
+    bad = tmp_path / "bad.txt"
+    bad.write_text("key 99 16 4 0 1.0\n")
+    with pytest.raises(capi.BackprojectorError) as e:
+        capi.tune_cache_load(bad)
+    assert e.value.status == capi.ERR_INVALID_ARGUMENT and ":1:" in str(e.value)
+    assert capi.tune_cache_size() == 2
+    capi.tune_cache_clear()
+    assert capi.tune_cache_size() == 0
