@@ -150,6 +150,26 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_tune_cache_load": (C.c_int, [C.c_char_p]),
     "bpgb_tune_cache_clear": (C.c_int, []),
     "bpgb_tune_cache_size": (C.c_int, []),
+    "bpgb_plan_execute_tiles": (C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, _P]),
+    "bpgb_plan_select_tiles": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_float, _P, _P, _P]),
+    "bpgb_synth_render_device": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_float, C.c_float, _P,
+                                           _P, C.c_uint64, _P, C.c_uint32, _P]),
+    "bpgb_block_max": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
+    "bpgb_upsample_trilinear": (C.c_int, [_P, _U32, _P, _U32, _P]),
+    "bpgb_laplacian7": (C.c_int, [_P, _U32, _P, _P]),
+    "bpgb_cnn_kp": (C.c_uint32, [C.c_uint32]),
+    "bpgb_cnn_conv3d": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, C.c_uint32,
+                                  C.c_int, _P, C.c_uint32, _P, _P, _P]),
+    "bpgb_cnn_wgrad_scratch_bytes": (C.c_uint64, [C.c_uint32, C.c_uint32, _U32, C.c_uint32]),
+    "bpgb_cnn_conv3d_wgrad": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P,
+                                        C.c_uint32, C.c_uint32, _P, C.c_uint64, _P, _P]),
+    "bpgb_cnn_pack_weights": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P, C.c_uint32,
+                                        _P, _P]),
+    "bpgb_cnn_bce_grad": (C.c_int, [_P, _P, C.c_uint64, C.c_float, C.c_float, _P, _P, _P]),
+    "bpgb_cnn_adam": (C.c_int, [_P, _P, _P, _P, C.c_uint64, C.c_float, C.c_float, C.c_float,
+                                C.c_float, C.c_uint32, _P]),
+    "bpgb_cnn_normalize": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
+    "bpgb_cnn_features": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
 }
 
 _lib = None
@@ -366,6 +386,20 @@ class Plan:
         st = lib().bpgb_plan_check(self.handle, C.byref(v))
         return st, int(v.value)
 
+    def execute_tiles(self, d_H, d_volume, d_tile_list, d_tile_count, max_tiles: int,
+                      stream=None) -> None:
+        check(lib().bpgb_plan_execute_tiles(self.handle, _ptr(d_H), _ptr(d_volume),
+                                            _ptr(d_tile_list), _ptr(d_tile_count), int(max_tiles),
+                                            _stream_ptr(stream)), "bpgb_plan_execute_tiles")
+
+    def select_tiles(self, d_score, block_dims, block_size: int, threshold: float, d_tile_list,
+                     d_tile_count, stream=None) -> None:
+        bd = np.asarray([int(v) for v in block_dims], np.uint32)
+        check(lib().bpgb_plan_select_tiles(self.handle, _ptr(d_score), u32ptr(bd), int(block_size),
+                                           float(threshold), _ptr(d_tile_list),
+                                           _ptr(d_tile_count), _stream_ptr(stream)),
+              "bpgb_plan_select_tiles")
+
     def dump_bins(self, voxel_ids, d_bins, stream=None) -> None:
         ids = np.ascontiguousarray(np.asarray(voxel_ids, dtype=np.int64))
         check(lib().bpgb_plan_dump_bins(self.handle, ids.ctypes.data_as(C.POINTER(C.c_int64)),
@@ -519,3 +553,90 @@ def tune_cache_clear() -> None:
 
 def tune_cache_size() -> int:
     return int(lib().bpgb_tune_cache_size())
+
+
+# ---------------------------------------------------------------- octree / CNN kernels
+
+def _dims(d) -> np.ndarray:
+    return np.asarray([int(v) for v in d], np.uint32)
+
+
+def synth_render_device(d_pairs, num_pairs: int, T: int, t0: float, deltaT: float, d_points,
+                        d_albedo, num_points: int, d_out, pitch: int | None = None,
+                        stream=None) -> None:
+    check(lib().bpgb_synth_render_device(_ptr(d_pairs), int(num_pairs), int(T), float(t0),
+                                         float(deltaT), _ptr(d_points), _ptr(d_albedo),
+                                         int(num_points), _ptr(d_out), int(pitch or T),
+                                         _stream_ptr(stream)), "bpgb_synth_render_device")
+
+
+def block_max(d_volume, voxels_per_side, block_size: int, d_out, stream=None) -> None:
+    check(lib().bpgb_block_max(_ptr(d_volume), u32ptr(_dims(voxels_per_side)), int(block_size),
+                               _ptr(d_out), _stream_ptr(stream)), "bpgb_block_max")
+
+
+def upsample_trilinear(d_coarse, coarse_dims, d_fine, fine_dims, stream=None) -> None:
+    check(lib().bpgb_upsample_trilinear(_ptr(d_coarse), u32ptr(_dims(coarse_dims)), _ptr(d_fine),
+                                        u32ptr(_dims(fine_dims)), _stream_ptr(stream)),
+          "bpgb_upsample_trilinear")
+
+
+def cnn_kp(cin: int) -> int:
+    return int(lib().bpgb_cnn_kp(int(cin)))
+
+
+def cnn_conv3d(d_X, cin: int, x_stride: int, dims, batch: int, d_Wt, np_: int, relu: bool,
+               d_Y=None, d_Yf=None, d_mask=None, mask_stride: int = 0, stream=None) -> None:
+    check(lib().bpgb_cnn_conv3d(_ptr(d_X), int(cin), int(x_stride), u32ptr(_dims(dims)), int(batch),
+                                _ptr(d_Wt), int(np_), 1 if relu else 0, _ptr(d_mask),
+                                int(mask_stride), _ptr(d_Y), _ptr(d_Yf), _stream_ptr(stream)),
+          "bpgb_cnn_conv3d")
+
+
+def cnn_wgrad_scratch_bytes(cin: int, np_: int, dims, batch: int) -> int:
+    return int(lib().bpgb_cnn_wgrad_scratch_bytes(int(cin), int(np_), u32ptr(_dims(dims)),
+                                                  int(batch)))
+
+
+def cnn_conv3d_wgrad(d_X, cin: int, x_stride: int, dims, batch: int, d_dY, np_: int, cout: int,
+                     d_scratch, scratch_bytes: int, d_dW, stream=None) -> None:
+    check(lib().bpgb_cnn_conv3d_wgrad(_ptr(d_X), int(cin), int(x_stride), u32ptr(_dims(dims)),
+                                      int(batch), _ptr(d_dY), int(np_), int(cout), _ptr(d_scratch),
+                                      int(scratch_bytes), _ptr(d_dW), _stream_ptr(stream)),
+          "bpgb_cnn_conv3d_wgrad")
+
+
+def cnn_pack_weights(d_W, cin: int, cout: int, np_: int, d_Wt, np_back: int = 0, d_Wb=None,
+                     stream=None) -> None:
+    check(lib().bpgb_cnn_pack_weights(_ptr(d_W), int(cin), int(cout), int(np_), _ptr(d_Wt),
+                                      int(np_back), _ptr(d_Wb), _stream_ptr(stream)),
+          "bpgb_cnn_pack_weights")
+
+
+def cnn_bce_grad(d_logits, d_labels, n: int, pos_weight: float, scale: float, d_dZ, d_loss=None,
+                 stream=None) -> None:
+    check(lib().bpgb_cnn_bce_grad(_ptr(d_logits), _ptr(d_labels), int(n), float(pos_weight),
+                                  float(scale), _ptr(d_dZ), _ptr(d_loss), _stream_ptr(stream)),
+          "bpgb_cnn_bce_grad")
+
+
+def cnn_adam(d_p, d_g, d_m, d_v, n: int, lr: float, beta1: float, beta2: float, eps: float,
+             step: int, stream=None) -> None:
+    check(lib().bpgb_cnn_adam(_ptr(d_p), _ptr(d_g), _ptr(d_m), _ptr(d_v), int(n), float(lr),
+                              float(beta1), float(beta2), float(eps), int(step),
+                              _stream_ptr(stream)), "bpgb_cnn_adam")
+
+
+def cnn_normalize(d_coarse, dims, batch: int, d_X, stream=None) -> None:
+    check(lib().bpgb_cnn_normalize(_ptr(d_coarse), u32ptr(_dims(dims)), int(batch), _ptr(d_X),
+                                   _stream_ptr(stream)), "bpgb_cnn_normalize")
+
+
+def laplacian7(d_volume, voxels_per_side, d_out, stream=None) -> None:
+    check(lib().bpgb_laplacian7(_ptr(d_volume), u32ptr(_dims(voxels_per_side)), _ptr(d_out),
+                                _stream_ptr(stream)), "bpgb_laplacian7")
+
+
+def cnn_features(d_coarse, dims, batch: int, d_X, stream=None) -> None:
+    check(lib().bpgb_cnn_features(_ptr(d_coarse), u32ptr(_dims(dims)), int(batch), _ptr(d_X),
+                                  _stream_ptr(stream)), "bpgb_cnn_features")

@@ -53,9 +53,12 @@ namespace bpgb {
 
 namespace {
 
-constexpr uint32_t kMaxChunk = 32;
+constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
-constexpr uint32_t kTableBytes = kMaxChunk * kRecordBytes;
+// row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
+__host__ __device__ constexpr uint32_t table_bytes_of(uint32_t c) {
+    return (c * kRecordBytes + 127) / 128 * 128;
+}
 constexpr float kMargin = 2.0f;                            // bins of slack around each window
 constexpr float kQEps = 1e-6f;                             // keeps q > 0 (bins^2)
 
@@ -79,6 +82,7 @@ struct FastArgs {
     uint32_t chunk;     // rows per stage
     uint32_t stages;
     uint32_t stage_bytes;
+    uint32_t table_bytes;  // row records at the start of each stage
     uint32_t align;     // TMA x alignment (elements)
     uint64_t L, S;
     uint32_t nchunks;   // ceil(S / chunk)
@@ -87,6 +91,10 @@ struct FastArgs {
     uint32_t T;
     float out_scale;
     uint64_t nvox;
+    // tile-list launches (block-sparse passes): CTA i runs tile tile_list[i] while
+    // i < *tile_count; null = every tile of the volume
+    const uint32_t *tile_list;
+    const uint32_t *tile_count;
 };
 
 struct TileGeo {
@@ -366,27 +374,37 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
                 (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
             unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
             float4 *table = reinterpret_cast<float4 *>(st);
-            const uint32_t data = smem_addr(st + kTableBytes);
+            const uint32_t data = smem_addr(st + a.table_bytes);
             const uint32_t fb = smem_addr(&full_bar[stage]);
-            int32_t lo = 0;
-            if (lane < nrows) {
-                const float4 G = spads[s0 + lane];
-                const float4 Lt = lasers[l];
-                float e[3], ew;
-                lo = row_record(a, g, G, Lt, e, ew);
-                const float ek = sel3(e[0], e[1], e[2], a.kax);
-                table[2 * lane] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
-                                              sel3(e[0], e[1], e[2], a.oax1), ew, ew);
-                table[2 * lane + 1] = make_float4(-ek, -ek, ew, ew);
+            // rows lane and lane + 32 of the chunk (kMaxChunk = 64)
+            int32_t lo[kMaxChunk / 32] = {};
+#pragma unroll
+            for (uint32_t q = 0; q < kMaxChunk / 32; q++) {
+                const uint32_t r = lane + 32 * q;
+                if (r < nrows) {
+                    const float4 G = spads[s0 + r];
+                    const float4 Lt = lasers[l];
+                    float e[3], ew;
+                    lo[q] = row_record(a, g, G, Lt, e, ew);
+                    const float ek = sel3(e[0], e[1], e[2], a.kax);
+                    table[2 * r] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
+                                               sel3(e[0], e[1], e[2], a.oax1), ew, ew);
+                    table[2 * r + 1] = make_float4(-ek, -ek, ew, ew);
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
             __syncwarp();
-            if (lane < nrows) {
-                const int32_t row = (int32_t)(row_base + l * a.S + s0 + lane);
-                const uint32_t dst = data + lane * a.row_bytes;
-                for (uint32_t b = 0; b < a.nbox; b++)
-                    tma_load_2d(dst + b * a.BW * esz, tmap, lo + (int32_t)(b * a.BW), row, fb);
+#pragma unroll
+            for (uint32_t q = 0; q < kMaxChunk / 32; q++) {
+                const uint32_t r = lane + 32 * q;
+                if (r < nrows) {
+                    const int32_t row = (int32_t)(row_base + l * a.S + s0 + r);
+                    const uint32_t dst = data + r * a.row_bytes;
+                    for (uint32_t b = 0; b < a.nbox; b++)
+                        tma_load_2d(dst + b * a.BW * esz, tmap, lo[q] + (int32_t)(b * a.BW), row,
+                                    fb);
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(fb);
@@ -478,7 +496,7 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
         const unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
         const float4 *table = reinterpret_cast<const float4 *>(st);
-        const uint32_t data = pad + stage * a.stage_bytes + kTableBytes;  // offset from smem_raw
+        const uint32_t data = pad + stage * a.stage_bytes + a.table_bytes;  // offset from smem_raw
 
         PairT part[NP];
         if (KAHAN) {
@@ -585,6 +603,14 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     __shared__ __align__(8) uint64_t full_bar[8];
     __shared__ __align__(8) uint64_t empty_bar[8];
     __shared__ int abort_flag;
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    uint32_t tile = (uint32_t)(blockIdx.x % ntiles), split = (uint32_t)(blockIdx.x / ntiles);
+    if (a.tile_list) {  // whole-CTA exits before any barrier is initialised
+        if (blockIdx.x >= *a.tile_count) return;
+        tile = a.tile_list[blockIdx.x];
+        split = 0;
+        if (tile >= ntiles) return;
+    }
     PipeShared sh;
     sh.smem_raw = smem_raw;
     sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;  // 128-byte aligned stage ring
@@ -601,11 +627,9 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
         mbar_fence_init();
     }
     __syncthreads();
-    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
     uint64_t step = 0;
-    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, out, diag,
-                                             (uint32_t)(blockIdx.x % ntiles),
-                                             (uint32_t)(blockIdx.x / ntiles), 0, step, sh);
+    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, out, diag, tile, split, 0,
+                                             step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
@@ -736,16 +760,20 @@ int encode_rows(CUtensorMap *map, int dtype, const void *d_H, uint32_t T, uint64
 // Tile presets: {lx, ly, lz, k, wx, wy, wz, kaxis, chunk, stages}.  The voxel line of a
 // thread runs along `kaxis`; lanes cover the other two axes.
 const FastConfig kPresets[] = {
-    {8, 1, 4, 8, 2, 1, 4, 1, 32, 4},  // 16 x 8 x 16, lanes over x-z, lines along y (depth)
-    {8, 4, 1, 8, 2, 2, 2, 2, 32, 4},  // 16 x 8 x 16, lanes over x-y, lines along z
-    {4, 1, 8, 8, 4, 1, 2, 1, 32, 4},  // 16 x 8 x 16, 4 x 8 lane blocks over x-z
-    {8, 1, 4, 8, 2, 2, 2, 1, 32, 4},  // 16 x 16 x 8
-    {8, 1, 4, 8, 4, 1, 2, 1, 32, 4},  // 32 x 8 x 8
-    {4, 1, 8, 8, 2, 1, 4, 1, 32, 4},  // 8 x 8 x 32
-    {8, 1, 4, 8, 1, 2, 4, 1, 32, 4},  // 8 x 16 x 16
-    {8, 1, 4, 16, 2, 1, 4, 1, 32, 4}, // 16 x 16 x 16, 16 voxels per thread
-    {8, 1, 4, 16, 1, 1, 8, 1, 32, 4}, // 8 x 16 x 32, 16 voxels per thread
-    {4, 1, 8, 16, 2, 1, 4, 1, 32, 4}, // 8 x 16 x 32, 4 x 8 lane blocks
+    {8, 1, 4, 8, 2, 1, 4, 1, 64, 4},  // 16 x 8 x 16, lanes over x-z, lines along y (depth)
+    {8, 4, 1, 8, 2, 2, 2, 2, 64, 4},  // 16 x 8 x 16, lanes over x-y, lines along z
+    {4, 1, 8, 8, 4, 1, 2, 1, 64, 4},  // 16 x 8 x 16, 4 x 8 lane blocks over x-z
+    {8, 1, 4, 8, 2, 2, 2, 1, 64, 4},  // 16 x 16 x 8
+    {8, 1, 4, 8, 4, 1, 2, 1, 64, 4},  // 32 x 8 x 8
+    {4, 1, 8, 8, 2, 1, 4, 1, 64, 4},  // 8 x 8 x 32
+    {8, 1, 4, 8, 1, 2, 4, 1, 64, 4},  // 8 x 16 x 16
+    {8, 1, 4, 16, 2, 1, 4, 1, 64, 4}, // 16 x 16 x 16, 16 voxels per thread
+    {8, 1, 4, 16, 1, 1, 8, 1, 64, 4}, // 8 x 16 x 32, 16 voxels per thread
+    {4, 1, 8, 16, 2, 1, 4, 1, 64, 4}, // 8 x 16 x 32, 4 x 8 lane blocks
+    // small tiles for block-sparse passes (2 or 4 consumer warps per CTA)
+    {8, 1, 4, 8, 1, 1, 2, 1, 64, 4},  // 8 x 8 x 8
+    {8, 1, 4, 8, 1, 1, 4, 1, 64, 4},  // 8 x 8 x 16
+    {8, 1, 4, 8, 2, 1, 2, 1, 64, 4},  // 16 x 8 x 8
 };
 
 template <typename HT, int K, bool PLANAR>
@@ -791,8 +819,10 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     };
     (void)t0;
     a = FastArgs{};
-    if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && (esz != 4 || kahan)) ||
-        cfg.lx * cfg.ly * cfg.lz != 32 || cfg.kaxis > 2 || cfg.wx * cfg.wy * cfg.wz != 8)
+    const uint32_t cwarps = cfg.wx * cfg.wy * cfg.wz;
+    if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && (esz != 4 || kahan || cwarps != 8)) ||
+        cfg.lx * cfg.ly * cfg.lz != 32 || cfg.kaxis > 2 ||
+        (cwarps != 8 && cwarps != 4 && cwarps != 2))
         return no("tile preset not available for this row type");
     const uint32_t lane[3] = {cfg.lx, cfg.ly, cfg.lz}, warp[3] = {cfg.wx, cfg.wy, cfg.wz};
     for (int k = 0; k < 3; k++) {
@@ -839,25 +869,35 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     if (a.BW > 256) return no("window box too wide");
     a.W = a.BW * a.nbox;
     a.row_bytes = a.W * esz;
-    auto stage_bytes = [&](uint32_t c) { return kTableBytes + c * a.row_bytes; };
+    auto stage_bytes = [&](uint32_t c) { return table_bytes_of(c) + c * a.row_bytes; };
     uint32_t chunk = (uint32_t)std::min<uint64_t>(
         std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, kMaxChunk), S);
     uint32_t stages = std::min<uint32_t>(stages_req ? stages_req : cfg.stages, 8);
     if (stages < 2) stages = 2;
     // Shared memory per CTA so that the variant's resident-CTA target fits one SM (228 KB).
-    const int ctas = fast_ctas_per_sm((int)cfg.k, kahan, (int)esz);
-    const uint32_t soft = ctas >= 3 ? 72 * 1024 : (ctas == 2 ? 110 * 1024 : 200 * 1024);
+    // Smaller CTAs (2 or 4 consumer warps, block-sparse tiles) need proportionally more
+    // resident CTAs per SM: 96 registers x (1 + warps) x 32 threads each.
+    const int ctas = cwarps == 8 ? fast_ctas_per_sm((int)cfg.k, kahan, (int)esz)
+                                 : (cwarps == 4 ? 4 : 7);
+    const uint32_t soft = ctas >= 7   ? 38 * 1024
+                          : ctas >= 4 ? 56 * 1024
+                          : ctas >= 3 ? 72 * 1024
+                          : (ctas == 2 ? 110 * 1024 : 200 * 1024);
     const uint32_t budget = 200 * 1024;
-    if (!chunk_req)
-        while (chunk > 4 && stages * stage_bytes(chunk) > soft) chunk = (chunk + 1) / 2;
+    // Long chunks amortise the per-stage handshake (measured: 8 -> 32 rows cut the
+    // 256^3 time by a quarter, pipeline depth 2..4 changed it by < 1%), so the depth
+    // gives way first.
     if (!stages_req)
         while (stages > 2 && stages * stage_bytes(chunk) > soft) stages--;
+    if (!chunk_req)
+        while (chunk > 4 && stages * stage_bytes(chunk) > soft) chunk = (chunk + 1) / 2;
     while (chunk > 1 && stages * stage_bytes(chunk) > budget) chunk = (chunk + 1) / 2;
     if (stages * stage_bytes(chunk) > budget)
         return no("time window of one tile does not fit in shared memory (" +
                   std::to_string(a.W) + " bins)");
     a.chunk = chunk;
     a.stages = stages;
+    a.table_bytes = table_bytes_of(chunk);
     a.stage_bytes = stage_bytes(chunk);
     a.nchunks = (uint32_t)((S + chunk - 1) / chunk);
     return BPGB_OK;
@@ -1071,6 +1111,84 @@ int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t s
         count_launches(1);
         BPGB_CUDA_TRY(cudaGetLastError());
     }
+    return BPGB_OK;
+}
+
+int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const uint32_t *d_list,
+                            const uint32_t *d_count, uint32_t max_tiles, cudaStream_t stream) {
+    const FastArgs &a0 = fp->a;
+    const uint64_t ntiles = (uint64_t)a0.tiles[0] * a0.tiles[1] * a0.tiles[2];
+    if (!d_list || !d_count) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null tile list");
+    if (a0.splits != 1)
+        return set_error(BPGB_ERR_UNSUPPORTED, "tile-list launches need a plan with pair_splits = 1");
+    if (max_tiles == 0) return BPGB_OK;
+    if (max_tiles > ntiles)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "max_tiles exceeds the plan's tile count");
+    if (((uintptr_t)d_H) % 16) return set_error(BPGB_ERR_INVALID_ARGUMENT, "H must be 16-byte aligned");
+    CUtensorMap map;
+    int st = encode_rows(&map, fp->dtype, d_H, a0.T, fp->P, fp->pitch, a0.BW);
+    if (st) return st;
+    FastArgs a = a0;
+    a.tile_list = d_list;
+    a.tile_count = d_count;
+    const float4 *spads = fp->d_tables;
+    const float4 *lasers = fp->d_tables + a.S;
+    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
+    void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&d_out,
+                    (void *)&fp->d_diag, (void *)&a};
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(max_tiles), dim3(fp->threads), args, fp->smem, stream));
+    count_launches(1);
+    return BPGB_OK;
+}
+
+namespace {
+
+// One thread per tile of the plan (tile order of tile_of_block): the tile is listed when
+// any score block it overlaps is above the threshold.  Blocks are bs^3 voxels on the
+// plan's voxel grid; list order depends on thread timing, results of a tile-list launch
+// do not (every tile is computed on its own).
+__global__ void select_tiles_kernel(const float *__restrict__ score, uint32_t bnx, uint32_t bny,
+                                    uint32_t bnz, uint32_t bs, float threshold, uint32_t t0n,
+                                    uint32_t t1n, uint32_t t2n, uint32_t d0, uint32_t d1,
+                                    uint32_t d2, uint32_t *__restrict__ list,
+                                    uint32_t *__restrict__ count) {
+    const uint32_t ntiles = t0n * t1n * t2n;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles;
+         t += gridDim.x * blockDim.x) {
+        const uint32_t tz = t % t2n, tx = (t / t2n) % t0n, ty = t / (t2n * t0n);
+        const uint32_t lo[3] = {tx * d0 / bs, ty * d1 / bs, tz * d2 / bs};
+        const uint32_t hi[3] = {min((tx * d0 + d0 - 1) / bs, bnx - 1),
+                                min((ty * d1 + d1 - 1) / bs, bny - 1),
+                                min((tz * d2 + d2 - 1) / bs, bnz - 1)};
+        bool any = false;
+        for (uint32_t x = lo[0]; x <= hi[0] && !any; x++)
+            for (uint32_t y = lo[1]; y <= hi[1] && !any; y++)
+                for (uint32_t z = lo[2]; z <= hi[2] && !any; z++)
+                    any = score[((uint64_t)x * bny + y) * bnz + z] > threshold;
+        if (any) list[atomicAdd(count, 1u)] = t;
+    }
+}
+
+}  // namespace
+
+int fast_plan_select_tiles(FastPlan *fp, const float *d_score, const uint32_t *block_dims,
+                           uint32_t block_size, float threshold, uint32_t *d_list,
+                           uint32_t *d_count, cudaStream_t stream) {
+    const FastArgs &a = fp->a;
+    if (!d_score || !block_dims || !d_list || !d_count || block_size == 0)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    for (int k = 0; k < 3; k++)
+        if (block_dims[k] == 0 || (uint64_t)block_dims[k] * block_size < a.n[k])
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "score blocks do not cover the volume");
+    const uint32_t ntiles = a.tiles[0] * a.tiles[1] * a.tiles[2];
+    BPGB_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), stream));
+    const unsigned blocks = (ntiles + 255) / 256;
+    select_tiles_kernel<<<blocks, 256, 0, stream>>>(d_score, block_dims[0], block_dims[1],
+                                                    block_dims[2], block_size, threshold,
+                                                    a.tiles[0], a.tiles[1], a.tiles[2], a.tdim[0],
+                                                    a.tdim[1], a.tdim[2], d_list, d_count);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
 }
 
@@ -1319,7 +1437,7 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     const uint32_t esz = dtype_bytes(o.h_dtype);
     const uint32_t bw = 128 / esz;
     FastConfig cfg = fast_preset(o.tile, o.h_dtype);
-    if (cfg.k != 8) cfg = fast_preset(0, o.h_dtype);
+    if (cfg.k != 8 || cfg.consumer_warps() != 8) cfg = fast_preset(0, o.h_dtype);
     auto *b = new bpgb_batch_s();
     b->n = n;
     b->dtype = o.h_dtype;
@@ -1408,9 +1526,11 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     uint32_t chunk = o.chunk > 0 ? std::min<uint32_t>((uint32_t)o.chunk, kMaxChunk) : cfg.chunk;
     uint32_t stages = o.stages > 0 ? std::min<uint32_t>((uint32_t)o.stages, 8) : cfg.stages;
     stages = std::max<uint32_t>(stages, 2);
-    auto stage_bytes = [&](uint32_t ch) { return kTableBytes + ch * max_row_bytes; };
-    while (chunk > 4 && stages * stage_bytes(chunk) > 110 * 1024) chunk = (chunk + 1) / 2;
-    while (stages > 2 && stages * stage_bytes(chunk) > 110 * 1024) stages--;
+    auto stage_bytes = [&](uint32_t ch) { return table_bytes_of(ch) + ch * max_row_bytes; };
+    if (o.stages <= 0)
+        while (stages > 2 && stages * stage_bytes(chunk) > 110 * 1024) stages--;
+    if (o.chunk <= 0)
+        while (chunk > 4 && stages * stage_bytes(chunk) > 110 * 1024) chunk = (chunk + 1) / 2;
     while (chunk > 1 && stages * stage_bytes(chunk) > 200 * 1024) chunk = (chunk + 1) / 2;
     if (stages * stage_bytes(chunk) > 200 * 1024) {
         batch_free(b);
@@ -1427,6 +1547,7 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         FastArgs &a = hc[c].a;
         a.chunk = chunk;
         a.stages = stages;
+        a.table_bytes = table_bytes_of(chunk);
         a.stage_bytes = stage_bytes(chunk);
         a.nchunks = (uint32_t)((a.S + chunk - 1) / chunk);
         a.planar = planar ? 1 : 0;

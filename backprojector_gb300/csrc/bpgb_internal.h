@@ -100,6 +100,11 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
 int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t stream);
 int fast_plan_dump_bins(FastPlan *fp, const int64_t *d_ids, int64_t n, int32_t *d_bins,
                         cudaStream_t stream);
+int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const uint32_t *d_list,
+                            const uint32_t *d_count, uint32_t max_tiles, cudaStream_t stream);
+int fast_plan_select_tiles(FastPlan *fp, const float *d_score, const uint32_t *block_dims,
+                           uint32_t block_size, float threshold, uint32_t *d_list,
+                           uint32_t *d_count, cudaStream_t stream);
 void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info);
 int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts);
 void fast_plan_free(FastPlan *fp);

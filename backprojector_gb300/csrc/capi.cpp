@@ -327,6 +327,31 @@ int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *str
     return BPGB_OK;
 }
 
+int bpgb_plan_execute_tiles(bpgb_plan plan, const void *d_H, void *d_volume,
+                            const uint32_t *d_tile_list, const uint32_t *d_tile_count,
+                            uint32_t max_tiles, void *stream) {
+    clear_error();
+    if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");
+    if (!d_volume || !d_H) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null buffer");
+    if (plan->algo != BPGB_ALGO_FAST || !plan->fast)
+        return set_error(BPGB_ERR_UNSUPPORTED, "tile-list launches need a FAST plan");
+    cudaStream_t s = (cudaStream_t)stream;
+    plan->last_stream = s;
+    return fast_plan_execute_tiles(plan->fast, d_H, d_volume, d_tile_list, d_tile_count,
+                                   max_tiles, s);
+}
+
+int bpgb_plan_select_tiles(bpgb_plan plan, const float *d_block_score,
+                           const uint32_t *block_dims, uint32_t block_size, float threshold,
+                           uint32_t *d_tile_list, uint32_t *d_tile_count, void *stream) {
+    clear_error();
+    if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");
+    if (plan->algo != BPGB_ALGO_FAST || !plan->fast)
+        return set_error(BPGB_ERR_UNSUPPORTED, "tile selection needs a FAST plan");
+    return fast_plan_select_tiles(plan->fast, d_block_score, block_dims, block_size, threshold,
+                                  d_tile_list, d_tile_count, (cudaStream_t)stream);
+}
+
 int bpgb_plan_check(bpgb_plan plan, uint64_t *violations) {
     clear_error();
     if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");

@@ -4,7 +4,7 @@
 //
 // Search (staged, so a 256^3 capture tunes in seconds):
 //   1. every tile preset the kernel family runs, at its own chunk and depth;
-//   2. chunk {8, 16, 32} x depth {2, 3, 4, 6} on the two fastest presets;
+//   2. chunk {16, 32, 64} x depth {2, 3, 4} on the two fastest presets;
 //   3. pair splits {1, 2, 4} on the winner (plans only; 0 = the plan's own choice).
 // Each candidate runs once untimed, then enough timed repetitions (CUDA events on the
 // caller's stream) to cover about 20 ms.  The winner is re-run with bin-window checking
@@ -112,8 +112,8 @@ int search(const std::vector<int> &tiles, bool try_splits, MakeTime &&make_and_t
               [](const Candidate &x, const Candidate &y) { return x.ms < y.ms; });
     const int top = std::min<int>(2, (int)ranked.size());
     for (int r = 0; r < top; r++)
-        for (int chunk : {8, 16, 32})
-            for (int stages : {2, 3, 4, 6}) trial(ranked[r].tile, chunk, stages, 0);
+        for (int chunk : {16, 32, 64})
+            for (int stages : {2, 3, 4}) trial(ranked[r].tile, chunk, stages, 0);
     auto fastest = [&]() {
         std::vector<Candidate> ok;
         for (const Candidate &c : all)
@@ -313,7 +313,8 @@ int bpgb_batch_autotune(const bpgb_capture_geometry *captures, uint32_t n, const
     };
     std::vector<int> tiles;
     for (int t = 0; t < fast_preset_count(); t++)
-        if (fast_preset(t, base.h_dtype).k == 8) tiles.push_back(t);
+        if (fast_preset(t, base.h_dtype).k == 8 && fast_preset(t, base.h_dtype).consumer_warps() == 8)
+            tiles.push_back(t);
     st = search(tiles, false, make_and_time, validate, &e, report);
     clear_error();
     if (st) return set_error(st, "autotune found no runnable configuration");
@@ -355,7 +356,7 @@ int bpgb_tune_cache_load(const char *path) {
         std::string key;
         TuneEntry e;
         if (!(in >> key >> e.tile >> e.chunk >> e.stages >> e.splits >> e.ms) ||
-            e.tile < -1 || e.tile >= fast_preset_count() || e.chunk < 0 || e.chunk > 32 ||
+            e.tile < -1 || e.tile >= fast_preset_count() || e.chunk < 0 || e.chunk > 64 ||
             e.stages < 0 || e.stages > 8 || e.splits < 0)
             return set_error(BPGB_ERR_INVALID_ARGUMENT,
                              std::string(path) + ":" + std::to_string(lineno) + ": bad entry");

@@ -1,0 +1,448 @@
+"""Learned octree: replaces the reference's threshold octree (octree_volume.hpp:18-198,
+backproject.hpp:264-335, backproject_cuda.cu:183-367) with a learned block proposal.
+
+Pipeline for one capture (all on the GPU, no host synchronisation inside):
+  1. coarse dense pass: the FAST kernel at 32^3 over the target box;
+  2. occupancy CNN (4 conv3d 3x3x3 layers, 1-16-16-16-1 channels, ReLU, BF16 weights
+     and activations, FP32 accumulation on the tensor cores) on the coarse volume
+     divided by its maximum: one logit per coarse voxel = per 8^3 block of the 256^3
+     target (the 32^3 grid and the 8^3 blocks tile the same box);
+  3. every fine voxel gets the trilinear upsampling of the coarse pass;
+  4. blocks scoring p >= p_lo are backprojected at full resolution (FAST kernel,
+     block-sparse tile-list launch): p >= p_hi confident, p_lo <= p < p_hi the
+     low-confidence band for which the dense pass is the fallback; p < p_lo keep step 3.
+
+Occupancy (labels and recall): voxel v of the dense reconstruction D is occupied when
+its negated 7-point Laplacian response F = -lap(D) (bpgb_laplacian7) reaches
+tau * max(F), tau = 0.2: the sharpened surfaces of the unfiltered backprojection, whose
+raw values are a broad low-frequency bump (on these scenes D >= 0.5 max(D) marks 13% of
+the voxels and 16% of the 8^3 blocks; F >= 0.2 max(F) marks 6.7% of the blocks).  A
+block is occupied when it holds an occupied voxel.  The CNN is trained only on dense reconstructions the plain FAST method makes
+from seeded synthetic scenes (synthetic.make_scene, octree_256 configuration).
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import capi, synthetic
+
+COARSE = 32
+BLOCK = 8
+TAU = 0.2
+IN_CHANNELS = 2  # coarse / max, and its negated 7-point Laplacian / max magnitude
+
+
+def layers(in_channels: int = IN_CHANNELS):
+    """(cin, cout, relu) of the four conv3d layers."""
+    return ((in_channels, 16, True), (16, 16, True), (16, 16, True), (16, 1, False))
+
+
+LAYERS = layers()
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "octree_cnn.npz"
+
+
+def _np(cout: int) -> int:
+    return 8 if cout <= 8 else 16
+
+
+class OccupancyCNN:
+    """The 4-layer occupancy CNN on the bpgb_cnn_* kernels (torch tensors hold memory)."""
+
+    def __init__(self, device, seed: int = 0, state: dict | None = None,
+                 in_channels: int = IN_CHANNELS):
+        import torch
+
+        self.torch = torch
+        self.device = device
+        if state is not None and "in_channels" in state:
+            in_channels = int(state["in_channels"])
+        self.in_channels = in_channels
+        self.layers = layers(in_channels)
+        self.W, self.M, self.V = [], [], []
+        rng = np.random.default_rng(seed)
+        for li, (cin, cout, _) in enumerate(self.layers):
+            kp = capi.cnn_kp(cin)
+            if state is not None:
+                w = np.asarray(state[f"w{li}"], np.float32)
+                assert w.shape == (kp, cout), (w.shape, kp, cout)
+            else:
+                w = np.zeros((kp, cout), np.float32)
+                fan_in = 27 * cin
+                w[:27 * cin] = rng.normal(0.0, math.sqrt(2.0 / fan_in), (27 * cin, cout))
+            self.W.append(torch.from_numpy(w).to(device))
+            self.M.append(torch.zeros_like(self.W[-1]))
+            self.V.append(torch.zeros_like(self.W[-1]))
+        self.step = int(state["step"]) if state is not None and "step" in state else 0
+        self.Wt, self.Wb = [], []
+        for li, (cin, cout, _) in enumerate(self.layers):
+            self.Wt.append(torch.zeros((_np(cout), capi.cnn_kp(cin)), dtype=torch.bfloat16,
+                                       device=device))
+            self.Wb.append(torch.zeros((16, capi.cnn_kp(cout)), dtype=torch.bfloat16,
+                                       device=device) if li > 0 else None)
+        self._bufs = {}
+        self.pack()
+
+    # ---- weights
+    def pack(self, stream=None):
+        for li, (cin, cout, _) in enumerate(self.layers):
+            capi.cnn_pack_weights(self.W[li], cin, cout, _np(cout), self.Wt[li],
+                                  16 if li > 0 else 0, self.Wb[li], stream)
+
+    def state(self) -> dict:
+        d = {f"w{li}": self.W[li].cpu().numpy() for li in range(len(self.layers))}
+        d["step"] = np.int64(self.step)
+        d["in_channels"] = np.int64(self.in_channels)
+        return d
+
+    def save(self, path, **meta) -> None:
+        path = Path(path)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        np.savez(path, **self.state(), **{k: np.asarray(v) for k, v in meta.items()})
+
+    @classmethod
+    def load(cls, device, path=WEIGHTS) -> tuple["OccupancyCNN", dict]:
+        z = np.load(path)
+        state = {k: z[k] for k in z.files}
+        return cls(device, state=state), state
+
+    # ---- buffers
+    def _buf(self, name, shape, dtype):
+        t = self._bufs.get(name)
+        if t is None or t.shape != shape or t.dtype != dtype:
+            t = self.torch.empty(shape, dtype=dtype, device=self.device)
+            self._bufs[name] = t
+        return t
+
+    # ---- passes
+    def features(self, coarse, dims, batch: int, X=None, stream=None):
+        """BF16 input [batch * prod(dims) * in_channels] of FP32 coarse volumes."""
+        n = batch * int(np.prod(dims)) * self.in_channels
+        if X is None:
+            X = self.torch.empty(n, dtype=self.torch.bfloat16, device=self.device)
+        if self.in_channels == 1:
+            capi.cnn_normalize(coarse, dims, batch, X, stream)
+        else:
+            capi.cnn_features(coarse, dims, batch, X, stream)
+        return X
+
+    def forward(self, X0, dims, batch: int, logits=None, stream=None):
+        """logits (FP32 [batch * prod(dims)]) of input features X0 (features())."""
+        torch = self.torch
+        V = batch * int(np.prod(dims))
+        Y1 = self._buf("Y1", (V, 16), torch.bfloat16)
+        Y2 = self._buf("Y2", (V, 16), torch.bfloat16)
+        Y3 = self._buf("Y3", (V, 16), torch.bfloat16)
+        if logits is None:
+            logits = self._buf("Z", (V,), torch.float32)
+        ci = self.in_channels
+        capi.cnn_conv3d(X0, ci, ci, dims, batch, self.Wt[0], 16, True, d_Y=Y1, stream=stream)
+        capi.cnn_conv3d(Y1, 16, 16, dims, batch, self.Wt[1], 16, True, d_Y=Y2, stream=stream)
+        capi.cnn_conv3d(Y2, 16, 16, dims, batch, self.Wt[2], 16, True, d_Y=Y3, stream=stream)
+        capi.cnn_conv3d(Y3, 16, 16, dims, batch, self.Wt[3], 8, False, d_Yf=logits, stream=stream)
+        return logits
+
+    def train_step(self, X0, labels, dims, batch: int, lr: float, pos_weight: float,
+                   stream=None):
+        """One Adam step on BCE-with-logits; returns the loss tensor (per voxel)."""
+        torch = self.torch
+        V = batch * int(np.prod(dims))
+        logits = self.forward(X0, dims, batch, stream=stream)
+        Y1, Y2, Y3 = self._bufs["Y1"], self._bufs["Y2"], self._bufs["Y3"]
+        dZ = self._buf("dZ", (V, 8), torch.bfloat16)
+        loss = self._buf("loss", (V,), torch.float32)
+        capi.cnn_bce_grad(logits, labels, V, pos_weight, 1.0 / V, dZ, loss, stream)
+        dY3 = self._buf("dY3", (V, 16), torch.bfloat16)
+        dY2 = self._buf("dY2", (V, 16), torch.bfloat16)
+        dY1 = self._buf("dY1", (V, 16), torch.bfloat16)
+        G = [self._buf(f"g{li}", tuple(self.W[li].shape), torch.float32)
+             for li in range(len(self.layers))]
+        ci = self.in_channels
+        nscr = max(capi.cnn_wgrad_scratch_bytes(16, 16, dims, batch),
+                   capi.cnn_wgrad_scratch_bytes(ci, 16, dims, batch))
+        scr = self._buf("scratch", (nscr // 4,), torch.float32)
+        capi.cnn_conv3d_wgrad(Y3, 16, 16, dims, batch, dZ, 8, 1, scr, nscr, G[3], stream)
+        capi.cnn_conv3d(dZ, 1, 8, dims, batch, self.Wb[3], 16, False, d_Y=dY3, d_mask=Y3,
+                        mask_stride=16, stream=stream)
+        capi.cnn_conv3d_wgrad(Y2, 16, 16, dims, batch, dY3, 16, 16, scr, nscr, G[2], stream)
+        capi.cnn_conv3d(dY3, 16, 16, dims, batch, self.Wb[2], 16, False, d_Y=dY2, d_mask=Y2,
+                        mask_stride=16, stream=stream)
+        capi.cnn_conv3d_wgrad(Y1, 16, 16, dims, batch, dY2, 16, 16, scr, nscr, G[1], stream)
+        capi.cnn_conv3d(dY2, 16, 16, dims, batch, self.Wb[1], 16, False, d_Y=dY1, d_mask=Y1,
+                        mask_stride=16, stream=stream)
+        capi.cnn_conv3d_wgrad(X0, ci, ci, dims, batch, dY1, 16, 16, scr, nscr, G[0], stream)
+        self.step += 1
+        for li in range(len(self.layers)):
+            capi.cnn_adam(self.W[li], G[li], self.M[li], self.V[li], self.W[li].numel(), lr, 0.9,
+                          0.999, 1e-8, self.step, stream)
+        self.pack(stream)
+        return loss
+
+
+# ---------------------------------------------------------------- capture geometry
+
+@dataclass
+class OctreeGeometry:
+    """The octree_256 capture geometry at the fine and coarse resolutions."""
+    pairs: np.ndarray
+    T: int
+    t0: float
+    deltaT: float
+    fine: tuple
+    coarse: tuple
+    zero: np.ndarray
+    inc_fine: np.ndarray
+    inc_coarse: np.ndarray
+    volume_position: np.ndarray
+    volume_size: np.ndarray
+    spec: synthetic.CaptureSpec = field(repr=False)
+
+    @classmethod
+    def of(cls, name: str = "octree_256", small: bool = False, **overrides) -> "OctreeGeometry":
+        c = synthetic.make_capture(name, seed=0, small=small, render=False, **overrides)
+        n = int(c.voxels_per_side[0])
+        coarse = n // BLOCK
+        zc, ic = capi.volume_basis(c.volume_position, c.volume_size,
+                                   np.full(3, coarse, np.uint32))
+        assert np.array_equal(zc, c.zero)
+        return cls(c.pairs, c.T, c.t0, c.deltaT, (n, n, n), (coarse, coarse, coarse), c.zero,
+                   c.inc, ic, c.volume_position, c.volume_size, c.spec)
+
+
+def scene(geo: OctreeGeometry, seed: int):
+    """Seeded scene points/albedo of the octree configuration (seed drives the scene)."""
+    rng = np.random.default_rng(seed)
+    lo = geo.volume_position.astype(np.float64) - geo.spec.volume_edge / 2
+    hi = geo.volume_position.astype(np.float64) + geo.spec.volume_edge / 2
+    return synthetic.make_scene(geo.spec, rng, lo, hi)
+
+
+class Reconstructor:
+    """Device state for rendering and reconstructing captures of one geometry."""
+
+    def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = None, **fine_opt):
+        import torch
+
+        self.torch = torch
+        self.geo = geo
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        P = len(geo.pairs)
+        self.d_pairs = torch.from_numpy(geo.pairs.view(np.uint8).copy()).to(device)
+        self.H = torch.empty((P, geo.T), dtype=torch.float32, device=device)
+        self.coarse = torch.empty(geo.coarse, dtype=torch.float32, device=device)
+        self.fine = torch.empty(geo.fine, dtype=torch.float32, device=device)
+        self.coarse_plan = capi.Plan(geo.pairs, geo.T, geo.coarse, geo.zero, geo.inc_coarse,
+                                     geo.t0, geo.deltaT, algo=capi.ALGO_FAST)
+        # The fine plan serves both the dense reference (execute) and the block-sparse
+        # pass (execute_tiles): FAST arithmetic is tile-relative, so one plan gives
+        # bit-identical voxels in both.
+        opt = dict(algo=capi.ALGO_FAST, pair_splits=1)
+        if fine_tile is not None:
+            opt["tile"] = fine_tile
+        opt.update(fine_opt)
+        self.sparse_plan = capi.Plan(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0,
+                                     geo.deltaT, **opt)
+        # labels only: the fastest dense configuration (its own tiles)
+        self.label_plan = capi.Plan(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0,
+                                    geo.deltaT, algo=capi.ALGO_FAST)
+        info = self.sparse_plan.info()
+        self.tile = tuple(info["tile"])
+        self.n_tiles = int(np.prod([-(-f // t) for f, t in zip(geo.fine, self.tile)]))
+        self.tile_list = torch.empty(self.n_tiles, dtype=torch.int32, device=device)
+        self.tile_count = torch.zeros(1, dtype=torch.int32, device=device)
+        self.blocks = geo.coarse
+        self.block_max = torch.empty(self.blocks, dtype=torch.float32, device=device)
+        self.X0 = torch.empty(int(np.prod(geo.coarse)) * 2, dtype=torch.bfloat16, device=device)
+        self.logits = torch.empty(int(np.prod(geo.coarse)), dtype=torch.float32, device=device)
+
+    def render(self, points: np.ndarray, albedo: np.ndarray) -> None:
+        torch = self.torch
+        dp = torch.from_numpy(np.ascontiguousarray(points, np.float32)).to(self.device)
+        da = torch.from_numpy(np.ascontiguousarray(albedo, np.float32)).to(self.device)
+        capi.synth_render_device(self.d_pairs, len(self.geo.pairs), self.geo.T, self.geo.t0,
+                                 self.geo.deltaT, dp, da, len(points), self.H,
+                                 stream=self.stream)
+        self.stream.synchronize()
+
+    def dense(self, out=None):
+        """Dense fine pass (synchronous: the result is ready on return)."""
+        out = self.fine if out is None else out
+        self.sparse_plan.execute(self.H, out, self.stream)
+        self.stream.synchronize()
+        return out
+
+    def computed_mask(self):
+        """Bool [fine] mask of the voxels the last reconstruct() backprojected."""
+        torch = self.torch
+        self.stream.synchronize()
+        n = int(self.tile_count.item())
+        ids = self.tile_list[:n].long()
+        nt = [-(-f // t) for f, t in zip(self.geo.fine, self.tile)]
+        tz = ids % nt[2]
+        tx = (ids // nt[2]) % nt[0]
+        ty = ids // (nt[2] * nt[0])
+        tmask = torch.zeros(nt, dtype=torch.bool, device=self.device)
+        tmask[tx, ty, tz] = True
+        m = tmask.repeat_interleave(self.tile[0], 0).repeat_interleave(self.tile[1], 1)
+        m = m.repeat_interleave(self.tile[2], 2)
+        return m[:self.geo.fine[0], :self.geo.fine[1], :self.geo.fine[2]]
+
+    def coarse_pass(self):
+        """Coarse pass (synchronous)."""
+        self.coarse_plan.execute(self.H, self.coarse, self.stream)
+        self.stream.synchronize()
+        return self.coarse
+
+    def labels_from_dense(self, dense) -> "torch.Tensor":
+        """Block maxima of the filtered dense volume F = -lap(D) divided by max(F)
+        ([32^3] FP32); a block is occupied where this reaches tau."""
+        filt = self._filtered(dense)
+        capi.block_max(filt, self.geo.fine, BLOCK, self.block_max, self.stream)
+        self.stream.synchronize()
+        return self.block_max / filt.max()
+
+    def _filtered(self, dense):
+        if getattr(self, "filt", None) is None:
+            self.filt = self.torch.empty(self.geo.fine, dtype=self.torch.float32,
+                                         device=self.device)
+        capi.laplacian7(dense, self.geo.fine, self.filt, self.stream)
+        self.stream.synchronize()
+        return self.filt
+
+    def occupied_voxels(self, dense, tau: float = TAU):
+        """Bool [fine] mask: F = -lap(dense) >= tau max(F)."""
+        f = self._filtered(dense)
+        return f >= tau * f.max()
+
+    def reconstruct(self, model: OccupancyCNN, logit_lo: float, out=None):
+        """Steps 1-4 of the module docstring on self.H, queued on self.stream (the
+        caller synchronises); returns the fine volume."""
+        out = self.fine if out is None else out
+        s = self.stream
+        self.coarse_plan.execute(self.H, self.coarse, s)
+        model.features(self.coarse, self.geo.coarse, 1, self.X0, s)
+        model.forward(self.X0, self.geo.coarse, 1, logits=self.logits, stream=s)
+        capi.upsample_trilinear(self.coarse, self.geo.coarse, out, self.geo.fine, s)
+        self.sparse_plan.select_tiles(self.logits, self.blocks, BLOCK, logit_lo, self.tile_list,
+                                      self.tile_count, s)
+        self.sparse_plan.execute_tiles(self.H, out, self.tile_list, self.tile_count,
+                                       self.n_tiles, s)
+        return out
+
+    def dense_for_labels(self, out=None):
+        """Dense fine pass with the label plan (synchronous)."""
+        out = self.fine if out is None else out
+        self.label_plan.execute(self.H, out, self.stream)
+        self.stream.synchronize()
+        return out
+
+    def close(self):
+        for p in (self.coarse_plan, self.sparse_plan, self.label_plan):
+            p.close()
+
+
+def logit(p: float) -> float:
+    return math.log(p / (1.0 - p))
+
+
+# ---------------------------------------------------------------- training data
+
+def make_training_set(rec: Reconstructor, n: int, seed0: int, log=print):
+    """Renders n seeded scenes, returns (coarse [n, 32^3] FP32, block_norm [n, 32^3] FP32):
+    the coarse pass and the dense pass's block maxima over its maximum."""
+    torch = rec.torch
+    nc = int(np.prod(rec.geo.coarse))
+    coarse = torch.empty((n, nc), dtype=torch.float32, device=rec.device)
+    bnorm = torch.empty((n, nc), dtype=torch.float32, device=rec.device)
+    t = time.perf_counter()
+    for i in range(n):
+        pts, alb = scene(rec.geo, seed0 + i)
+        rec.render(pts, alb)
+        coarse[i] = rec.coarse_pass().reshape(-1)
+        bnorm[i] = rec.labels_from_dense(rec.dense_for_labels()).reshape(-1)
+        if log and (i + 1) % 200 == 0:
+            log(f"  scenes {i + 1}/{n} ({time.perf_counter() - t:.1f} s)")
+    rec.stream.synchronize()
+    return coarse, bnorm
+
+
+def train(model: OccupancyCNN, coarse, bnorm, dims, epochs: int = 30, batch: int = 16,
+          lr: float = 2e-3, tau: float = TAU, seed: int = 0, max_pos_weight: float = 50.0,
+          log=print) -> list[float]:
+    torch = model.torch
+    n = coarse.shape[0]
+    nc = coarse.shape[1]
+    labels = (bnorm >= tau).to(torch.uint8)
+    pos = float(labels.float().mean().item())
+    pos_weight = min(max_pos_weight, (1.0 - pos) / max(pos, 1e-6))
+    X = model.features(coarse, dims, n).reshape(n, -1)
+    rng = np.random.default_rng(seed)
+    hist = []
+    for ep in range(epochs):
+        order = rng.permutation(n)
+        rate = lr * 0.5 * (1.0 + math.cos(math.pi * ep / epochs))
+        tot = 0.0
+        for b0 in range(0, n - batch + 1, batch):
+            idx = torch.from_numpy(order[b0:b0 + batch]).to(model.device)
+            xb = X.index_select(0, idx).reshape(-1).contiguous()
+            yb = labels.index_select(0, idx).reshape(-1).contiguous()
+            loss = model.train_step(xb, yb, dims, batch, rate, pos_weight)
+            tot += float(loss.sum().item())
+        steps = max(1, n // batch)
+        hist.append(tot / steps)
+        if log:
+            log(f"  epoch {ep + 1}/{epochs} loss {hist[-1]:.4f} (pos {pos:.4f}, w {pos_weight:.1f})")
+    return hist
+
+
+def block_scores(model: OccupancyCNN, coarse, dims):
+    """Sigmoid scores [n, 32^3] of the model over a set of coarse volumes."""
+    torch = model.torch
+    n, nc = coarse.shape
+    X = model.features(coarse, dims, n).reshape(n, -1)
+    out = torch.empty((n, nc), dtype=torch.float32, device=model.device)
+    for i in range(n):
+        model.forward(X[i], dims, 1, logits=out[i])
+    torch.cuda.synchronize()
+    return torch.sigmoid(out)
+
+
+def calibrate(scores, bnorm, tau: float = TAU, recall: float = 0.995) -> float:
+    """Largest p_lo whose block recall of occupied blocks on (scores, bnorm) >= recall."""
+    occ = bnorm >= tau
+    s = scores[occ]
+    if s.numel() == 0:
+        return 0.5
+    q = float(np.quantile(s.float().cpu().numpy(), 1.0 - recall))
+    return max(min(q, 0.5), 1e-6)
+
+
+def metrics(out, dense, computed, occ_vox, block: int = BLOCK) -> dict:
+    """Octree volume vs a dense reference (same grid): occupied-voxel recall (occupied
+    voxels, `occ_vox`, that the octree backprojected at full resolution, `computed`),
+    rel-L2 over all voxels and over occupied blocks, PSNR, computed fraction."""
+    import torch as T
+
+    d = dense.double()
+    o = out.double()
+    mx = float(d.max())
+    exact = computed
+    n = d.shape[0] // block
+    bl = occ_vox.reshape(n, block, n, block, n, block).any(dim=5).any(dim=3).any(dim=1)
+    occ_blocks = bl.repeat_interleave(block, 0).repeat_interleave(block, 1).repeat_interleave(block, 2)
+    diff = o - d
+    res = {
+        "occupied_voxels": int(occ_vox.sum()),
+        "recall": float((exact & occ_vox).sum()) / max(1, int(occ_vox.sum())),
+        "rel_l2": float(T.linalg.vector_norm(diff) / T.linalg.vector_norm(d)),
+        "rel_l2_occupied_blocks": float(T.linalg.vector_norm(diff[occ_blocks]) /
+                                        max(1e-300, float(T.linalg.vector_norm(d[occ_blocks])))),
+        "psnr_db": float(10.0 * math.log10(mx * mx / max(1e-300, float((diff * diff).mean())))),
+        "computed_fraction": float(computed.float().mean()),
+    }
+    return res

@@ -86,7 +86,7 @@ typedef struct bpgb_options {
     int32_t pair_splits; /* CTAs sharing one voxel tile over disjoint pair ranges (0 = auto) */
     int32_t checked;     /* 1 = clamp and count out-of-window bins (tests) */
     uint32_t spin_limit; /* bounded mbarrier waits: polls before giving up (0 = default) */
-    int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..32 (0 = from the preset) */
+    int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..64 (0 = from the preset) */
     int32_t stages;      /* FAST: pipeline depth, 2..8 (0 = from the preset) */
     int32_t reserved[5];
 } bpgb_options;
@@ -124,7 +124,8 @@ uint64_t bpgb_launch_count(void);
  * transient_size = P * T elements, the voxel volume [Nx, Ny, Nz] (x slowest) is
  * OVERWRITTEN, the call is synchronous on the current device.  Unlike the reference,
  * every pair is used (it skips the last P mod blockDim pairs) and every voxel is
- * visited for any N (its voxel cursor skips voxels when N is not a multiple of 16).
+ * visited exactly once for any N (its voxel cursor wraps and recomputes some voxels
+ * when N is not a multiple of 16, backproject_cuda.cu:65-80).
  * ALGO_AUTO, FP32 accumulation.  Replaces backproject_cuda.cu:370-500 / 671-801. */
 int bpgb_backproject_f32(const float *transient_chunk, uint64_t transient_size, uint32_t T,
                          const bpgb_pair *scanned_pairs, uint64_t num_pairs,
@@ -155,6 +156,22 @@ int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_
                      const float *volume_zero_pos, const float *voxel_inc, float t0,
                      float deltaT, const bpgb_options *opt);
 int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *stream);
+/* Block-sparse form of bpgb_plan_execute (FAST plans with pair_splits = 1): computes
+ * only the voxel tiles listed in device memory, d_tile_list[0 .. *d_tile_count), and
+ * leaves every other voxel of d_volume untouched.  max_tiles bounds *d_tile_count and
+ * sets the launch size, so the call reads no device value on the host and can be
+ * captured in a CUDA graph.  Tile ids follow the plan's tile grid
+ * (bpgb_plan_info.tile voxels per tile; id = (ty * tiles_x + tx) * tiles_z + tz). */
+int bpgb_plan_execute_tiles(bpgb_plan plan, const void *d_H, void *d_volume,
+                            const uint32_t *d_tile_list, const uint32_t *d_tile_count,
+                            uint32_t max_tiles, void *stream);
+/* Fills the tile list for bpgb_plan_execute_tiles from a score grid of
+ * block_size^3-voxel blocks (float [bx, by, bz], x slowest, covering the volume): a tile
+ * is listed when any block it overlaps scores above `threshold`.  Zeroes *d_tile_count
+ * first (stream-ordered). */
+int bpgb_plan_select_tiles(bpgb_plan plan, const float *d_block_score,
+                           const uint32_t *block_dims, uint32_t block_size, float threshold,
+                           uint32_t *d_tile_list, uint32_t *d_tile_count, void *stream);
 /* Synchronises the plan's last stream and reports device-side diagnostics: returns
  * BPGB_ERR_TIMEOUT if a bounded wait gave up, BPGB_ERR_WINDOW if checked mode counted
  * out-of-window bins (count in *violations when non-null), else BPGB_OK. */
@@ -244,12 +261,73 @@ int bpgb_batch_graph_launch(bpgb_batch batch, const void *d_H, float *d_volumes,
 int bpgb_batch_check(bpgb_batch batch, uint64_t *violations);
 int bpgb_batch_destroy(bpgb_batch batch);
 
+/* ---- learned octree: block scores, fill, occupancy CNN ---------------------------
+ * Replace the reference's threshold octree (octree_volume.hpp:18-198,
+ * backproject.hpp:264-335; GPU backproject_cuda.cu:183-367, 503-669, which prints "NOT
+ * WORKING YET"): a coarse dense pass feeds a small 3D CNN that scores 8^3-voxel blocks
+ * of the fine volume; bpgb_plan_select_tiles + bpgb_plan_execute_tiles run the fine
+ * pass on the scored blocks only.  Volumes are float [n0, n1, n2], x slowest. */
+
+/* out[b] = max of d_volume over block b (block_size^3 voxels, edge blocks clipped);
+ * out is float [ceil(n0/bs), ceil(n1/bs), ceil(n2/bs)]. */
+int bpgb_block_max(const float *d_volume, const uint32_t *voxels_per_side, uint32_t block_size,
+                   float *d_out, void *stream);
+/* d_out[v] = sum over v's in-volume face neighbours u of (vol[v] - vol[u]): the negated
+ * 7-point Laplacian filter (positive at local maxima, the usual sharpening of
+ * unfiltered backprojections).  d_out must not alias d_volume. */
+int bpgb_laplacian7(const float *d_volume, const uint32_t *voxels_per_side, float *d_out,
+                    void *stream);
+/* d_fine = trilinear interpolation of d_coarse, both grids spanning one box with spacing
+ * size / (n - 1) (the reference's voxel_inc, backproject.hpp:834-839). */
+int bpgb_upsample_trilinear(const float *d_coarse, const uint32_t *coarse_dims, float *d_fine,
+                            const uint32_t *fine_dims, void *stream);
+
+/* Occupancy CNN kernels: 3x3x3 convolutions, zero padding, BF16 activations and weights,
+ * FP32 accumulation on the tensor cores (mma.sync m16n8k16).  Activations are
+ * channels-last BF16 [batch * n0 * n1 * n2][stride].  A layer with cin inputs has
+ * K = 27 cin + 1 GEMM rows padded to bpgb_cnn_kp(cin): row t * cin + c = tap t
+ * (offsets t/9-1, t/3%3-1, t%3-1 along x, y, z), input channel c; row 27 cin = bias.
+ * Weights: FP32 master W[kp][cout]; packed BF16 Wt[np][kp] (np = cout padded to 8/16)
+ * and, for the backward-data pass, Wb[np_back][kp(cout)] (taps flipped, channels
+ * transposed, no bias) from bpgb_cnn_pack_weights.
+ * conv3d: Y = act(conv(X, W)) with act = ReLU when relu != 0, then, when d_mask is set,
+ * Y[v][c] = 0 wherever mask[v][c] <= 0 (ReLU backward); d_Y BF16 [V][np] and/or d_Yf =
+ * channel 0 in FP32 [V].  (cin, np) in {(1,16), (2,16), (16,16), (16,8)}. */
+uint32_t bpgb_cnn_kp(uint32_t cin);
+int bpgb_cnn_conv3d(const void *d_X, uint32_t cin, uint32_t x_stride, const uint32_t *dims,
+                    uint32_t batch, const void *d_Wt, uint32_t np, int relu, const void *d_mask,
+                    uint32_t mask_stride, void *d_Y, float *d_Yf, void *stream);
+/* dW[kp][cout] (FP32) = sum over voxels of im2col(X) x dY (dY BF16 [V][np]); partial
+ * sums per 2048 voxels in d_scratch, reduced in a fixed order (deterministic). */
+uint64_t bpgb_cnn_wgrad_scratch_bytes(uint32_t cin, uint32_t np, const uint32_t *dims,
+                                      uint32_t batch);
+int bpgb_cnn_conv3d_wgrad(const void *d_X, uint32_t cin, uint32_t x_stride, const uint32_t *dims,
+                          uint32_t batch, const void *d_dY, uint32_t np, uint32_t cout,
+                          float *d_scratch, uint64_t scratch_bytes, float *d_dW, void *stream);
+int bpgb_cnn_pack_weights(const float *d_W, uint32_t cin, uint32_t cout, uint32_t np,
+                          void *d_Wt, uint32_t np_back, void *d_Wb, void *stream);
+/* BCE with logits: dZ[v][0..7] = (w (sigmoid(z) - y) scale, 0, ..., 0) BF16 (16-byte rows),
+ * w = pos_weight where y = 1; d_loss (optional) = w (softplus(z) - y z) scale per v. */
+int bpgb_cnn_bce_grad(const float *d_logits, const uint8_t *d_labels, uint64_t n,
+                      float pos_weight, float scale, void *d_dZ, float *d_loss, void *stream);
+/* Adam (bias-corrected, step >= 1) on FP32 parameters. */
+int bpgb_cnn_adam(float *d_p, const float *d_g, float *d_m, float *d_v, uint64_t n, float lr,
+                  float beta1, float beta2, float eps, uint32_t step, void *stream);
+/* d_X (BF16 [batch * n0 n1 n2]) = each sample of d_coarse divided by its maximum. */
+int bpgb_cnn_normalize(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
+                       void *stream);
+/* Two input channels per voxel, d_X BF16 [batch * n0 n1 n2][2]: the sample divided by
+ * its maximum, and its negated 7-point Laplacian (as bpgb_laplacian7) divided by its
+ * largest magnitude. */
+int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
+                      void *stream);
+
 /* ---- autotuner -------------------------------------------------------------------
  * No counterpart in the reference (its launch shape is fixed: 16^3 voxels per launch,
  * the largest power-of-two block not above the pair count).  Times FAST configurations
  * on the caller's device buffers (contents are read, results are overwritten) on
  * `stream`, in three stages: every tile preset at its own chunk and depth; chunk
- * {8,16,32} x depth {2,3,4,6} on the two fastest presets; pair splits {1,2,4} on the
+ * {16,32,64} x depth {2,3,4} on the two fastest presets; pair splits {1,2,4} on the
  * winner (plans only).  The winner is re-run with bin-window checking; a candidate
  * that puts any bin outside its window is never chosen.  On return opt->tile, chunk,
  * stages and pair_splits hold the choice (and opt->algo = FAST for plans); the other

@@ -1,0 +1,347 @@
+"""Learned-octree kernels against plain PyTorch FP32 references of the same ops, and the
+block-sparse reconstruction against the dense FAST pass.
+
+Tolerances: BF16 outputs (conv3d forward / backward-data) within 1e-2 relative of the
+FP32 reference on BF16-exact inputs (one BF16 rounding of an FP32 sum); FP32 outputs
+(weight gradients) within 1e-3; the block-sparse fine pass equals the dense pass
+bit for bit on every tile it computes (same kernel arithmetic per tile)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from backprojector_gb300 import capi, octree, synthetic
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+CONV_CASES = [(1, 16, True, 16), (2, 16, True, 16), (16, 16, True, 16), (16, 1, False, 8)]
+
+
+def bf16_exact(t):
+    return t.bfloat16().float()
+
+
+def torch_weight(Wm, cin, cout):
+    import torch
+
+    w = Wm[:27 * cin].reshape(3, 3, 3, cin, cout).permute(4, 3, 0, 1, 2).contiguous()
+    b = Wm[27 * cin].clone()
+    return w, b
+
+
+def random_master(cin, cout, seed, device):
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    kp = capi.cnn_kp(cin)
+    W = torch.zeros((kp, cout))
+    W[:27 * cin + 1] = torch.randn((27 * cin + 1, cout), generator=g) * 0.3
+    return bf16_exact(W).to(device)
+
+
+@pytest.mark.parametrize("cin,cout,relu,np_", CONV_CASES)
+def test_conv3d_forward_vs_torch(cuda, cin, cout, relu, np_):
+    import torch
+    import torch.nn.functional as F
+
+    dims, batch = (6, 5, 7), 2
+    g = torch.Generator().manual_seed(cin * 100 + cout)
+    X = bf16_exact(torch.randn((batch, *dims, cin), generator=g))
+    W = random_master(cin, cout, 7, cuda)
+    Wt = torch.empty((np_, capi.cnn_kp(cin)), dtype=torch.bfloat16, device=cuda)
+    capi.cnn_pack_weights(W, cin, cout, np_, Wt)
+    dX = X.reshape(-1, cin).to(cuda).bfloat16().contiguous()
+    V = batch * int(np.prod(dims))
+    Y = torch.zeros((V, np_), dtype=torch.bfloat16, device=cuda)
+    Yf = torch.zeros(V, device=cuda)
+    capi.cnn_conv3d(dX, cin, cin, dims, batch, Wt, np_, relu, d_Y=Y, d_Yf=Yf)
+    torch.cuda.synchronize()
+    w, b = torch_weight(W.cpu(), cin, cout)
+    ref = F.conv3d(X.permute(0, 4, 1, 2, 3), w, b, padding=1)
+    if relu:
+        ref = ref.clamp_min(0)
+    ref = ref.permute(0, 2, 3, 4, 1).reshape(V, cout)
+    got = Y.float().cpu()[:, :cout]
+    assert torch.allclose(got, ref, rtol=1e-2, atol=1e-2 * float(ref.abs().max())), \
+        float((got - ref).abs().max())
+    assert torch.allclose(Yf.cpu(), ref[:, 0], rtol=1e-5, atol=1e-4 * float(ref.abs().max()))
+    if np_ > cout:
+        assert torch.all(Y.float().cpu()[:, cout:] == (0 if not relu else 0))
+
+
+@pytest.mark.parametrize("cin,cout,relu,np_", CONV_CASES)
+def test_conv3d_weight_and_input_gradients_vs_torch(cuda, cin, cout, relu, np_):
+    import torch
+    import torch.nn.functional as F
+
+    dims, batch = (5, 6, 4), 3
+    V = batch * int(np.prod(dims))
+    g = torch.Generator().manual_seed(5 + cin + cout)
+    X = bf16_exact(torch.randn((batch, *dims, cin), generator=g))
+    dY = bf16_exact(torch.randn((batch, *dims, cout), generator=g))
+    W = random_master(cin, cout, 11, cuda)
+    # weight gradient (bias row included)
+    dX = X.reshape(V, cin).to(cuda).bfloat16().contiguous()
+    dYp = torch.zeros((V, np_), dtype=torch.bfloat16, device=cuda)
+    dYp[:, :cout] = dY.reshape(V, cout).to(cuda).bfloat16()
+    nscr = capi.cnn_wgrad_scratch_bytes(cin, np_, dims, batch)
+    scr = torch.empty(nscr // 4, device=cuda)
+    dW = torch.full(tuple(W.shape), float("nan"), device=cuda)
+    capi.cnn_conv3d_wgrad(dX, cin, cin, dims, batch, dYp, np_, cout, scr, nscr, dW)
+    torch.cuda.synchronize()
+    w, b = torch_weight(W.cpu(), cin, cout)
+    xt = X.permute(0, 4, 1, 2, 3).clone().requires_grad_(True)
+    wt = w.clone().requires_grad_(True)
+    bt = b.clone().requires_grad_(True)
+    out = F.conv3d(xt, wt, bt, padding=1)
+    out.backward(dY.permute(0, 4, 1, 2, 3))
+    ref_w = wt.grad.permute(2, 3, 4, 1, 0).reshape(27 * cin, cout)
+    got = dW.cpu()
+    scale = float(ref_w.abs().max())
+    assert torch.allclose(got[:27 * cin], ref_w, rtol=1e-3, atol=1e-4 * scale)
+    assert torch.allclose(got[27 * cin], bt.grad, rtol=1e-3, atol=1e-4 * float(bt.grad.abs().max()))
+    assert torch.all(got[27 * cin + 1:] == 0)
+    # input gradient: the forward kernel on dY with the backward weights and a ReLU mask
+    if cin == 16:
+        Wt = torch.empty((np_, capi.cnn_kp(cin)), dtype=torch.bfloat16, device=cuda)
+        Wb = torch.empty((16, capi.cnn_kp(cout)), dtype=torch.bfloat16, device=cuda)
+        capi.cnn_pack_weights(W, cin, cout, np_, Wt, 16, Wb)
+        mask = bf16_exact(torch.randn((V, 16), generator=g)).to(cuda).bfloat16()
+        gX = torch.zeros((V, 16), dtype=torch.bfloat16, device=cuda)
+        capi.cnn_conv3d(dYp, cout, np_, dims, batch, Wb, 16, False, d_Y=gX, d_mask=mask,
+                        mask_stride=16)
+        torch.cuda.synchronize()
+        ref_x = xt.grad.permute(0, 2, 3, 4, 1).reshape(V, cin) * (mask.float().cpu() > 0)
+        gotx = gX.float().cpu()
+        assert torch.allclose(gotx, ref_x, rtol=1e-2, atol=1e-2 * float(ref_x.abs().max()))
+
+
+def test_bce_and_adam_vs_torch(cuda):
+    import torch
+
+    n = 1000
+    g = torch.Generator().manual_seed(3)
+    z = (torch.randn(n, generator=g) * 3).to(cuda)
+    y = (torch.rand(n, generator=g) < 0.2).to(torch.uint8).to(cuda)
+    dZ = torch.empty((n, 8), dtype=torch.bfloat16, device=cuda)
+    loss = torch.empty(n, device=cuda)
+    capi.cnn_bce_grad(z, y, n, 4.0, 1.0 / n, dZ, loss)
+    torch.cuda.synchronize()
+    zr = z.cpu().clone().requires_grad_(True)
+    w = torch.where(y.cpu() > 0, 4.0, 1.0)
+    lr_ = (w * torch.nn.functional.binary_cross_entropy_with_logits(
+        zr, y.cpu().float(), reduction="none")) / n
+    lr_.sum().backward()
+    assert torch.allclose(loss.cpu(), lr_.detach(), rtol=1e-5, atol=1e-9)
+    assert torch.allclose(dZ[:, 0].float().cpu(), zr.grad, rtol=1e-2, atol=1e-6)
+    assert torch.all(dZ[:, 1:].float() == 0)
+    # Adam, three steps against torch.optim.Adam
+    p0 = torch.randn(300, generator=g)
+    p = p0.clone().to(cuda)
+    m = torch.zeros_like(p)
+    v = torch.zeros_like(p)
+    ref = p0.clone().requires_grad_(True)
+    opt = torch.optim.Adam([ref], lr=1e-2, betas=(0.9, 0.999), eps=1e-8)
+    for step in range(1, 4):
+        grad = torch.randn(300, generator=g)
+        capi.cnn_adam(p, grad.to(cuda), m, v, 300, 1e-2, 0.9, 0.999, 1e-8, step)
+        ref.grad = grad.clone()
+        opt.step()
+    torch.cuda.synchronize()
+    assert torch.allclose(p.cpu(), ref.detach(), rtol=1e-5, atol=1e-6)
+
+
+def test_device_renderer_matches_host_renderer(cuda):
+    import torch
+
+    c = synthetic.make_capture("octree_256", seed=3, small=True)
+    H = torch.empty((c.P, c.T + 64), device=cuda)
+    dp = torch.from_numpy(c.pairs.view(np.uint8).copy()).to(cuda)
+    capi.synth_render_device(dp, c.P, c.T, c.t0, c.deltaT, torch.from_numpy(c.points).to(cuda),
+                             torch.from_numpy(c.albedo).to(cuda), len(c.points), H, c.T + 64)
+    torch.cuda.synchronize()
+    got = H.cpu().numpy()
+    assert np.all(got[:, c.T:] == 0)
+    got = got[:, :c.T]
+    # same hits up to FP32 path rounding: totals per pair agree; a hit moves to the next
+    # bin when its FP32 path lies within rounding of a bin edge (~1e-4 of 30,000 hits per
+    # pair here, each changing two of the pair's 1,024 bins)
+    assert np.allclose(got.sum(1), c.H.sum(1), rtol=1e-5)
+    changed = np.abs(got - c.H) > 1e-5 * np.abs(c.H).max()
+    assert changed.mean() < 1e-2
+    assert oracle.rel_l2(got, c.H) < 5e-2
+    # deterministic
+    H2 = torch.empty_like(H)
+    capi.synth_render_device(dp, c.P, c.T, c.t0, c.deltaT, torch.from_numpy(c.points).to(cuda),
+                             torch.from_numpy(c.albedo).to(cuda), len(c.points), H2, c.T + 64)
+    torch.cuda.synchronize()
+    assert torch.equal(H, H2)
+
+
+def test_cnn_features_vs_torch(cuda):
+    import torch
+    import torch.nn.functional as F
+
+    g = torch.Generator().manual_seed(9)
+    dims, batch = (6, 7, 5), 2
+    coarse = torch.rand((batch, *dims), generator=g)
+    X = torch.empty((batch * int(np.prod(dims)) * 2,), dtype=torch.bfloat16, device=cuda)
+    capi.cnn_features(coarse.to(cuda), dims, batch, X)
+    torch.cuda.synchronize()
+    got = X.float().cpu().reshape(batch, *dims, 2)
+    k = torch.zeros((1, 1, 3, 3, 3))
+    for d in ((0, 1, 1), (2, 1, 1), (1, 0, 1), (1, 2, 1), (1, 1, 0), (1, 1, 2)):
+        k[0, 0][d] = 1.0
+    cnt = F.conv3d(torch.ones((1, 1, *dims)), k, padding=1)[0, 0]
+    for b in range(batch):
+        c = coarse[b]
+        lap = cnt * c - F.conv3d(c[None, None], k, padding=1)[0, 0]
+        assert torch.allclose(got[b, ..., 0], (c / c.max()).bfloat16().float())
+        ref1 = (lap / lap.abs().max()).bfloat16().float()
+        assert torch.allclose(got[b, ..., 1], ref1, atol=1e-2)
+
+
+def test_laplacian7_vs_torch(cuda):
+    import torch
+    import torch.nn.functional as F
+
+    g = torch.Generator().manual_seed(4)
+    vol = torch.randn((9, 7, 11), generator=g)
+    out = torch.empty_like(vol).to(cuda)
+    capi.laplacian7(vol.to(cuda), (9, 7, 11), out)
+    torch.cuda.synchronize()
+    # sum over in-volume neighbours of (c - n): 6-neighbour count x c minus neighbour sum
+    ones = torch.ones((1, 1, 9, 7, 11))
+    k = torch.zeros((1, 1, 3, 3, 3))
+    for d in ((0, 1, 1), (2, 1, 1), (1, 0, 1), (1, 2, 1), (1, 1, 0), (1, 1, 2)):
+        k[0, 0][d] = 1.0
+    nsum = F.conv3d(vol[None, None], k, padding=1)[0, 0]
+    cnt = F.conv3d(ones, k, padding=1)[0, 0]
+    ref = cnt * vol - nsum
+    assert torch.allclose(out.cpu(), ref, rtol=1e-5, atol=1e-5)
+
+
+def test_block_max_and_upsample(cuda):
+    import torch
+    import torch.nn.functional as F
+
+    g = torch.Generator().manual_seed(1)
+    vol = torch.randn((20, 16, 12), generator=g)
+    out = torch.empty((3, 2, 2), device=cuda)
+    capi.block_max(vol.to(cuda), (20, 16, 12), 8, out)
+    torch.cuda.synchronize()
+    ref = F.max_pool3d(F.pad(vol[None, None], (0, 4, 0, 0, 0, 4), value=-1e30), 8)[0, 0]
+    assert torch.equal(out.cpu(), ref)
+    coarse = torch.randn((4, 5, 3), generator=g)
+    fine = torch.empty((10, 13, 7), device=cuda)
+    capi.upsample_trilinear(coarse.to(cuda), (4, 5, 3), fine, (10, 13, 7))
+    torch.cuda.synchronize()
+    ref = F.interpolate(coarse[None, None], size=(10, 13, 7), mode="trilinear",
+                        align_corners=True)[0, 0]
+    assert torch.allclose(fine.cpu(), ref, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("tile", [10, 11, 12])
+def test_small_tile_presets_vs_oracle(cuda, tile):
+    import torch
+
+    c = synthetic.make_capture("octree_256", seed=5, small=True)
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    dH = torch.from_numpy(c.H).to(cuda)
+    dV = torch.empty(tuple(int(v) for v in c.voxels_per_side), device=cuda)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST, tile=tile, checked=1) as p:
+        p.execute(dH, dV)
+        assert p.check() == 0
+        assert p.info()["threads"] in (96, 160)
+    assert oracle.rel_l2(dV.cpu().numpy(), ref) < 5e-3
+
+
+@pytest.mark.parametrize("tile", [0, 10])
+def test_tile_list_execution_matches_dense(cuda, tile):
+    import torch
+
+    c = synthetic.make_capture("octree_256", seed=6, small=True)
+    dH = torch.from_numpy(c.H).to(cuda)
+    N = tuple(int(v) for v in c.voxels_per_side)
+    dense = torch.empty(N, device=cuda)
+    with capi.Plan(c.pairs, c.T, N, c.zero, c.inc, c.t0, c.deltaT, algo=capi.ALGO_FAST,
+                   tile=tile, pair_splits=1) as p:
+        p.execute(dH, dense)
+        info = p.info()
+        td = info["tile"]
+        nt = [-(-n // t) for n, t in zip(N, td)]
+        ntiles = int(np.prod(nt))
+        # score blocks: every other 8^3 block
+        nb = [n // 8 for n in N]
+        score = torch.zeros(nb, device=cuda)
+        score.view(-1)[::2] = 1.0
+        lst = torch.empty(ntiles, dtype=torch.int32, device=cuda)
+        cnt = torch.zeros(1, dtype=torch.int32, device=cuda)
+        p.select_tiles(score, nb, 8, 0.5, lst, cnt)
+        out = torch.full(N, float("nan"), device=cuda)
+        p.execute_tiles(dH, out, lst, cnt, ntiles)
+        p.check()
+    n_sel = int(cnt.item())
+    assert 0 < n_sel <= ntiles
+    sel = sorted(lst[:n_sel].cpu().tolist())
+    assert len(set(sel)) == n_sel
+    o, d = out.cpu().numpy(), dense.cpu().numpy()
+    computed = ~np.isnan(o)
+    # computed voxels = exactly the selected tiles, bit-identical to the dense pass
+    mask = np.zeros(N, bool)
+    for t in sel:
+        tz = t % nt[2]
+        tx = (t // nt[2]) % nt[0]
+        ty = t // (nt[2] * nt[0])
+        mask[tx * td[0]:(tx + 1) * td[0], ty * td[1]:(ty + 1) * td[1], tz * td[2]:(tz + 1) * td[2]] = True
+    assert np.array_equal(computed, mask)
+    assert np.array_equal(o[mask], d[mask])
+    # every selected tile overlaps a scored block, every scored block is covered
+    sc = score.cpu().numpy().repeat(8, 0).repeat(8, 1).repeat(8, 2) > 0.5
+    assert np.all(mask[sc])
+
+
+def test_octree_pipeline_limits(cuda):
+    """Untrained model: p_lo = 0 computes every block (equals dense); p_lo -> 1 computes
+    none (the trilinear fill of the coarse pass)."""
+    import torch
+
+    geo = octree.OctreeGeometry.of("octree_256", small=True)
+    rec = octree.Reconstructor(geo, cuda, fine_tile=10)
+    model = octree.OccupancyCNN(cuda, seed=1)
+    pts, alb = octree.scene(geo, 7)
+    rec.render(pts, alb)
+    dense = rec.dense().clone()
+    out = rec.reconstruct(model, -1e30)
+    rec.stream.synchronize()
+    out = out.clone()
+    assert torch.equal(out, dense)
+    m = octree.metrics(out, dense, rec.computed_mask(), rec.occupied_voxels(dense))
+    assert m["recall"] == 1.0 and m["rel_l2"] == 0.0 and m["computed_fraction"] == 1.0
+    out2 = rec.reconstruct(model, 1e30)
+    rec.stream.synchronize()
+    out2 = out2.clone()
+    assert not rec.computed_mask().any()
+    fill = torch.empty_like(dense)
+    capi.upsample_trilinear(rec.coarse, geo.coarse, fill, geo.fine, rec.stream)
+    rec.stream.synchronize()
+    torch.cuda.synchronize()
+    assert torch.equal(out2, fill)
+    rec.close()
+
+
+def test_cnn_training_reduces_loss(cuda):
+    import torch
+
+    model = octree.OccupancyCNN(cuda, seed=0)
+    dims, n = (8, 8, 8), 8
+    g = torch.Generator().manual_seed(0)
+    coarse = torch.rand((n, 512), generator=g).to(cuda)
+    bnorm = coarse.clone()  # the label is a threshold of the input itself
+    hist = octree.train(model, coarse, bnorm, dims, epochs=40, batch=4, lr=5e-3, tau=0.7,
+                        log=None)
+    assert hist[-1] < 0.5 * hist[0], hist
