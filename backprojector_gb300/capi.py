@@ -157,6 +157,10 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_block_max": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
     "bpgb_upsample_trilinear": (C.c_int, [_P, _U32, _P, _U32, _P]),
     "bpgb_laplacian7": (C.c_int, [_P, _U32, _P, _P]),
+    "bpgb_rows_absmax": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, _P, _P]),
+    "bpgb_rows_to_half": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P,
+                                    C.c_float, C.c_int, _P, C.c_uint32, _P]),
+    "bpgb_volume_scale": (C.c_int, [_P, C.c_uint64, C.c_float, _P, C.c_float, _P]),
     "bpgb_cnn_kp": (C.c_uint32, [C.c_uint32]),
     "bpgb_cnn_conv3d": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, C.c_uint32,
                                   C.c_int, _P, C.c_uint32, _P, _P, _P]),
@@ -640,3 +644,21 @@ def laplacian7(d_volume, voxels_per_side, d_out, stream=None) -> None:
 def cnn_features(d_coarse, dims, batch: int, d_X, stream=None) -> None:
     check(lib().bpgb_cnn_features(_ptr(d_coarse), u32ptr(_dims(dims)), int(batch), _ptr(d_X),
                                   _stream_ptr(stream)), "bpgb_cnn_features")
+
+
+def rows_absmax(d_H, rows: int, T: int, pitch: int, d_max, stream=None) -> None:
+    check(lib().bpgb_rows_absmax(_ptr(d_H), int(rows), int(T), int(pitch), _ptr(d_max),
+                                 _stream_ptr(stream)), "bpgb_rows_absmax")
+
+
+def rows_to_half(d_H, rows: int, T: int, in_pitch: int, dtype: int, d_out, out_pitch: int,
+                 scale: float = 1.0, d_absmax=None, target: float = 0.0, stream=None) -> None:
+    check(lib().bpgb_rows_to_half(_ptr(d_H), int(rows), int(T), int(in_pitch), float(scale),
+                                  _ptr(d_absmax), float(target), int(dtype), _ptr(d_out),
+                                  int(out_pitch), _stream_ptr(stream)), "bpgb_rows_to_half")
+
+
+def volume_scale(d_volume, n: int, scale: float = 1.0, d_absmax=None, target: float = 0.0,
+                 stream=None) -> None:
+    check(lib().bpgb_volume_scale(_ptr(d_volume), int(n), float(scale), _ptr(d_absmax),
+                                  float(target), _stream_ptr(stream)), "bpgb_volume_scale")

@@ -221,27 +221,41 @@ def scene(geo: OctreeGeometry, seed: int):
     return synthetic.make_scene(geo.spec, rng, lo, hi)
 
 
-class Reconstructor:
-    """Device state for rendering and reconstructing captures of one geometry."""
+H_TARGET = 16384.0  # FP16 rows: the capture's largest |H| maps to this value
 
-    def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = None, **fine_opt):
+
+class Reconstructor:
+    """Device state for rendering and reconstructing captures of one geometry.
+
+    Rows are stored as `h_dtype` (FP16 by default: each capture divided by
+    max|H| / H_TARGET, computed and applied on the device; the volumes are multiplied
+    back at the end of each pass)."""
+
+    def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = 10,
+                 h_dtype: int = capi.DTYPE_F16, **fine_opt):
         import torch
 
         self.torch = torch
         self.geo = geo
         self.device = device
+        self.h_dtype = h_dtype
         self.stream = torch.cuda.Stream(device=device)
         P = len(geo.pairs)
         self.d_pairs = torch.from_numpy(geo.pairs.view(np.uint8).copy()).to(device)
         self.H = torch.empty((P, geo.T), dtype=torch.float32, device=device)
+        self.absmax = torch.ones(1, dtype=torch.float32, device=device)
+        if h_dtype == capi.DTYPE_F16:
+            self.rows = torch.empty((P, geo.T), dtype=torch.float16, device=device)
+        else:
+            self.rows = self.H
         self.coarse = torch.empty(geo.coarse, dtype=torch.float32, device=device)
         self.fine = torch.empty(geo.fine, dtype=torch.float32, device=device)
         self.coarse_plan = capi.Plan(geo.pairs, geo.T, geo.coarse, geo.zero, geo.inc_coarse,
-                                     geo.t0, geo.deltaT, algo=capi.ALGO_FAST)
+                                     geo.t0, geo.deltaT, algo=capi.ALGO_FAST, h_dtype=h_dtype)
         # The fine plan serves both the dense reference (execute) and the block-sparse
         # pass (execute_tiles): FAST arithmetic is tile-relative, so one plan gives
         # bit-identical voxels in both.
-        opt = dict(algo=capi.ALGO_FAST, pair_splits=1)
+        opt = dict(algo=capi.ALGO_FAST, pair_splits=1, h_dtype=h_dtype)
         if fine_tile is not None:
             opt["tile"] = fine_tile
         opt.update(fine_opt)
@@ -267,12 +281,27 @@ class Reconstructor:
         capi.synth_render_device(self.d_pairs, len(self.geo.pairs), self.geo.T, self.geo.t0,
                                  self.geo.deltaT, dp, da, len(points), self.H,
                                  stream=self.stream)
+        self.ingest()
+
+    def ingest(self) -> None:
+        """Stores self.H (FP32) as the plans' row type (synchronous)."""
+        if self.h_dtype == capi.DTYPE_F16:
+            P, T = self.H.shape
+            capi.rows_absmax(self.H, P, T, T, self.absmax, self.stream)
+            capi.rows_to_half(self.H, P, T, T, capi.DTYPE_F16, self.rows, T,
+                              d_absmax=self.absmax, target=H_TARGET, stream=self.stream)
         self.stream.synchronize()
+
+    def _unscale(self, vol) -> None:
+        if self.h_dtype == capi.DTYPE_F16:
+            capi.volume_scale(vol, vol.numel(), d_absmax=self.absmax, target=H_TARGET,
+                              stream=self.stream)
 
     def dense(self, out=None):
         """Dense fine pass (synchronous: the result is ready on return)."""
         out = self.fine if out is None else out
-        self.sparse_plan.execute(self.H, out, self.stream)
+        self.sparse_plan.execute(self.rows, out, self.stream)
+        self._unscale(out)
         self.stream.synchronize()
         return out
 
@@ -294,9 +323,9 @@ class Reconstructor:
 
     def coarse_pass(self):
         """Coarse pass (synchronous)."""
-        self.coarse_plan.execute(self.H, self.coarse, self.stream)
+        self.coarse_plan.execute(self.rows, self.coarse, self.stream)
         self.stream.synchronize()
-        return self.coarse
+        return self.coarse  # in stored-row units (the CNN input is scale-free)
 
     def labels_from_dense(self, dense) -> "torch.Tensor":
         """Block maxima of the filtered dense volume F = -lap(D) divided by max(F)
@@ -324,14 +353,15 @@ class Reconstructor:
         caller synchronises); returns the fine volume."""
         out = self.fine if out is None else out
         s = self.stream
-        self.coarse_plan.execute(self.H, self.coarse, s)
+        self.coarse_plan.execute(self.rows, self.coarse, s)
         model.features(self.coarse, self.geo.coarse, 1, self.X0, s)
         model.forward(self.X0, self.geo.coarse, 1, logits=self.logits, stream=s)
         capi.upsample_trilinear(self.coarse, self.geo.coarse, out, self.geo.fine, s)
         self.sparse_plan.select_tiles(self.logits, self.blocks, BLOCK, logit_lo, self.tile_list,
                                       self.tile_count, s)
-        self.sparse_plan.execute_tiles(self.H, out, self.tile_list, self.tile_count,
+        self.sparse_plan.execute_tiles(self.rows, out, self.tile_list, self.tile_count,
                                        self.n_tiles, s)
+        self._unscale(out)
         return out
 
     def dense_for_labels(self, out=None):

@@ -1,6 +1,6 @@
 """Trains the occupancy CNN of the learned octree on seeded synthetic scenes.
 
-    python -m backprojector_gb300.octree_train [--scenes 2000] [--epochs 30] [--out PATH]
+    python -m backprojector_gb300.octree_train [--scenes 2000] [--epochs 60] [--out PATH]
 
 Data: scene i (seed seed0 + i, octree_256 configuration: one laser, 128 x 128 SPADs,
 T = 4096, 1-5 spheres / boxes / tori of 10,000 surface points) is rendered on the GPU
@@ -25,7 +25,7 @@ def main(argv=None) -> dict:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--scenes", type=int, default=2000)
     ap.add_argument("--seed0", type=int, default=1_000_000)
-    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--tau", type=float, default=octree.TAU)

@@ -34,6 +34,9 @@ WORKLOADS = {
     "precision_64": "dense, 1 laser x 64x64 SPADs, T=2048, dT=1mm, 64^3 over a 1 m cube",
     "dense_exhaustive_16": "dense, 16x16 lasers x 16x16 SPADs, T=512, dT=3mm, 32^3 over 0.5 m",
     "phasor_128": "phasor complex64, 1 laser x 128x128 SPADs, T=4096, dT=0.5mm, 128^3 over 1.5 m",
+    "octree_256_learned": "learned octree on the octree_256 capture shape: 32^3 coarse pass, "
+                          "BF16 tensor-core occupancy CNN, trilinear fill, block-sparse 8^3 "
+                          "fine pass; FP16 rows; dense-equivalent updates/s (V x P / time)",
     "batch_64": "64 uneven captures in one persistent launch replayed from a CUDA graph: SPAD "
                 "grids {16,32,48,64,96}^2 (1 laser, or 16^2 x 16^2 exhaustive for a quarter), "
                 "T {512,1024,2048}, volumes {32,48,64,96}^3, 4-40 scatterers, FP16 rows with a "
@@ -129,7 +132,8 @@ def run_reference_arm(args):
 
     if args.workload == "batch_64":
         return run_reference_arm_batch(args)
-    cap = synthetic.make_capture(args.workload, seed=args.seed)
+    name = "octree_256" if args.workload == "octree_256_learned" else args.workload
+    cap = synthetic.make_capture(name, seed=args.seed)
     for _ in range(args.warmup):
         cpu_baseline(cap, args.ref_sample, seed=1)
     rates, secs = [], []
@@ -344,6 +348,191 @@ def run_ours(args):
     plan.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_octree(args):
+    """octree_256_learned: each step reconstructs one of several seeded test captures
+    (FP16 rows resident) through the learned octree; quality against the dense pass
+    (same kernel and tiles, FP16 rows), the FP32 dense pass and the FP64 oracle (voxel
+    sample)."""
+    import torch
+
+    from backprojector_gb300 import capi, octree
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if not octree.WEIGHTS.exists():
+        raise RuntimeError(f"{octree.WEIGHTS} missing: run python -m backprojector_gb300.octree_train")
+    model, state = octree.OccupancyCNN.load(dev)
+    p_lo = float(state["p_lo"])
+    logit_lo = octree.logit(p_lo)
+    geo = octree.OctreeGeometry.of("octree_256")
+    rec = octree.Reconstructor(geo, dev)
+    P = len(geo.pairs)
+    nvox = int(np.prod(geo.fine))
+    n_test = 6
+    scenes = []
+    quality = []
+    oracle_err = []
+    for k in range(n_test):
+        pts, alb = octree.scene(geo, 2_000_000 + args.seed * 100 + k)
+        rec.render(pts, alb)
+        rows, amax = rec.rows.clone(), rec.absmax.clone()
+        dense16 = rec.dense().clone()
+        out = rec.reconstruct(model, logit_lo)
+        rec.stream.synchronize()
+        out = out.clone()  # the reconstructor's buffer is reused by the dense passes below
+        comp = rec.computed_mask()
+        occ = rec.occupied_voxels(dense16)
+        m = octree.metrics(out, dense16, comp, occ)
+        dense32 = rec.dense_for_labels().clone()
+        d32 = dense32.double()
+        m["rel_l2_vs_fp32_dense"] = float(torch.linalg.vector_norm(out.double() - d32) /
+                                          torch.linalg.vector_norm(d32))
+        m["rel_l2_occupied_vs_fp32_dense"] = float(
+            torch.linalg.vector_norm(out.double()[occ] - d32[occ]) /
+            torch.linalg.vector_norm(d32[occ]))
+        quality.append(m)
+        if k < 2 and rank == 0:
+            from oracle import oracle
+
+            ids_all = torch.nonzero(occ.reshape(-1)).reshape(-1)
+            g = torch.Generator(device="cpu").manual_seed(k)
+            pick = ids_all[torch.randperm(len(ids_all), generator=g)[:256].to(ids_all.device)]
+            ids = np.sort(pick.cpu().numpy())
+            ref = oracle.bp_gpu_f64(rec.H.cpu().numpy(), geo.pairs, geo.fine, geo.zero,
+                                    geo.inc_fine, geo.t0, geo.deltaT, voxels=ids)
+            got = out.reshape(-1)[torch.from_numpy(ids).to(dev)].double().cpu().numpy()
+            oracle_err.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        scenes.append((rows, amax))
+        del dense16, dense32
+    torch.cuda.synchronize()
+
+    def step(k):
+        rec.rows, rec.absmax = scenes[k % n_test]
+        rec.reconstruct(model, logit_lo)
+
+    for k in range(args.warmup):
+        step(k)
+    rec.stream.synchronize()
+    torch.cuda.synchronize()
+    launches0 = capi.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(rec.stream)
+        for k in range(args.steps):
+            step(k)
+        e1.record(rec.stream)
+        e1.synchronize()
+    launches = capi.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    value = nvox * P / (ms * 1e-3)
+
+    # stage breakdown on scene 0
+    rec.rows, rec.absmax = scenes[0]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    s = rec.stream
+    ev[0].record(s)
+    rec.coarse_plan.execute(rec.rows, rec.coarse, s)
+    ev[1].record(s)
+    model.features(rec.coarse, geo.coarse, 1, rec.X0, s)
+    model.forward(rec.X0, geo.coarse, 1, logits=rec.logits, stream=s)
+    ev[2].record(s)
+    capi.upsample_trilinear(rec.coarse, geo.coarse, rec.fine, geo.fine, s)
+    rec.sparse_plan.select_tiles(rec.logits, rec.blocks, octree.BLOCK, logit_lo, rec.tile_list,
+                                 rec.tile_count, s)
+    ev[3].record(s)
+    rec.sparse_plan.execute_tiles(rec.rows, rec.fine, rec.tile_list, rec.tile_count,
+                                  rec.n_tiles, s)
+    ev[4].record(s)
+    rec._unscale(rec.fine)
+    ev[5].record(s)
+    ev[5].synchronize()
+    names = ["coarse_pass", "cnn", "fill_select", "sparse_fine_pass", "rescale"]
+    stages = {n: ev[i].elapsed_time(ev[i + 1]) for i, n in enumerate(names)}
+    n_sel = int(rec.tile_count.item())
+    computed_updates = n_sel * int(np.prod(rec.tile)) * P
+
+    # plain dense baselines on the same GPU (FP32 and FP16 rows, default FAST plans)
+    def time_plan(p, H, out, reps=3):
+        p.execute(H, out, s)
+        s.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            p.execute(H, out, s)
+        b.record(s)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    pts, alb = octree.scene(geo, 2_000_000 + args.seed * 100)
+    rec.render(pts, alb)
+    with capi.Plan(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0, geo.deltaT,
+                   algo=capi.ALGO_FAST) as p32:
+        dense32_ms = time_plan(p32, rec.H, rec.fine)
+    with capi.Plan(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0, geo.deltaT,
+                   algo=capi.ALGO_FAST, h_dtype=capi.DTYPE_F16) as p16:
+        dense16_ms = time_plan(p16, rec.rows, rec.fine)
+
+    # e2e: FP16 rows and their scale from pinned host memory, volume back, every step
+    hrows = scenes[0][0].cpu().pin_memory()
+    hmax = scenes[0][1].cpu().pin_memory()
+    hvol = torch.empty(geo.fine, dtype=torch.float32).pin_memory()
+    drows = torch.empty_like(scenes[0][0])
+    dmax = torch.empty_like(scenes[0][1])
+
+    def e2e_step():
+        with torch.cuda.stream(s):
+            drows.copy_(hrows, non_blocking=True)
+            dmax.copy_(hmax, non_blocking=True)
+            rec.rows, rec.absmax = drows, dmax
+            out = rec.reconstruct(model, logit_lo)
+            hvol.copy_(out, non_blocking=True)
+        s.synchronize()
+
+    e2e_step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t) / args.steps
+
+    clocks = clk.summary()
+    sparse_ms = stages["sparse_fine_pass"]
+    roofline = roofline_for(computed_updates / (sparse_ms * 1e-3), sparse_ms,
+                            hrows.numel() * 2 + n_sel * int(np.prod(rec.tile)) * 4, False, clocks,
+                            dev, "bp_fast_kernel (8^3 tiles, tile-list launch)")
+    q = {k: float(np.mean([m[k] for m in quality])) for k in quality[0]}
+    q["recall_min"] = float(min(m["recall"] for m in quality))
+    q["fp64_oracle_rel_l2_occupied_sample"] = oracle_err
+    line = {
+        "metric": "voxel-pair updates/s (dense-equivalent: 256^3 x 16384 per reconstruction)",
+        "value": value, "unit": "updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16 storage, f32 accumulate; bf16 CNN",
+        "data": "synthetic (seeded octree_256 scenes rendered on the GPU; no dataset available)",
+        "config": {"workload": f"octree_256_learned: {WORKLOADS['octree_256_learned']}",
+                   "test_scenes": n_test, "p_lo": p_lo, "tau": float(state["tau"]),
+                   "l2": "inputs larger than L2 (FP16 rows 134 MB per capture, 6 captures)",
+                   "parallelism": "single GPU"},
+        "ms_per_recon": {"learned_octree": ms, "dense_fp32": dense32_ms, "dense_fp16": dense16_ms,
+                         "speedup_vs_dense_fp32": dense32_ms / ms,
+                         "speedup_vs_dense_fp16": dense16_ms / ms},
+        "stages_ms_scene0": stages, "selected_tiles_scene0": n_sel, "tiles": rec.n_tiles,
+        "computed_updates_per_s_sparse_pass": computed_updates / (sparse_ms * 1e-3),
+        "quality": q,
+        "roofline": roofline,
+        "e2e": {"value": nvox * P / e2e_s, "unit": "updates/s (dense-equivalent)",
+                "h2d_bytes_per_step": int(hrows.numel() * 2 + 4),
+                "d2h_bytes_per_step": int(hvol.numel() * 4), "ms_per_step": e2e_s * 1e3,
+                "path": "FP16 rows H2D + learned-octree reconstruction + volume D2H"},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    rec.close()
 
 
 def run_batch(args):
@@ -593,6 +782,8 @@ def main():
         run_reference_arm(args)
     elif args.workload == "batch_64":
         run_batch(args)
+    elif args.workload == "octree_256_learned":
+        run_octree(args)
     else:
         run_ours(args)
 

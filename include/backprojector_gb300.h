@@ -261,6 +261,21 @@ int bpgb_batch_graph_launch(bpgb_batch batch, const void *d_H, float *d_volumes,
 int bpgb_batch_check(bpgb_batch batch, uint64_t *violations);
 int bpgb_batch_destroy(bpgb_batch batch);
 
+/* ---- FP16 / BF16 row storage -------------------------------------------------------
+ * *d_max (device float) = max |H| over rows x T (NaN counts as +inf); rows of `pitch`.
+ * bpgb_rows_to_half: d_out[r][t] = H[r][t] / s as FP16 or BF16 (dtype), bins
+ * T..out_pitch-1 zero, with s = scale, or s = *d_absmax / target read on the device when
+ * d_absmax is non-null (so a capture is scaled without a host round trip).  A FAST plan
+ * then either takes h_scale = s, or runs with h_scale = 1 and bpgb_volume_scale
+ * (same s arguments) multiplies the volume back. */
+int bpgb_rows_absmax(const float *d_H, uint64_t rows, uint32_t T, uint32_t pitch,
+                     float *d_max, void *stream);
+int bpgb_rows_to_half(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch, float scale,
+                      const float *d_absmax, float target, int dtype, void *d_out,
+                      uint32_t out_pitch, void *stream);
+int bpgb_volume_scale(float *d_volume, uint64_t n, float scale, const float *d_absmax,
+                      float target, void *stream);
+
 /* ---- learned octree: block scores, fill, occupancy CNN ---------------------------
  * Replace the reference's threshold octree (octree_volume.hpp:18-198,
  * backproject.hpp:264-335; GPU backproject_cuda.cu:183-367, 503-669, which prints "NOT

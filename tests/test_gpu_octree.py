@@ -224,6 +224,30 @@ def test_laplacian7_vs_torch(cuda):
     assert torch.allclose(out.cpu(), ref, rtol=1e-5, atol=1e-5)
 
 
+@pytest.mark.parametrize("dtype", ["f16", "bf16"])
+def test_rows_to_half_with_device_scale(cuda, dtype):
+    import torch
+
+    g = torch.Generator().manual_seed(2)
+    H = (torch.rand((37, 100), generator=g) * 1e5).to(cuda)
+    H[3, 7] = -2.5e5
+    mx = torch.empty(1, device=cuda)
+    capi.rows_absmax(H, 37, 90, 100, mx)
+    out = torch.full((37, 96), 7.0, dtype=torch.float16 if dtype == "f16" else torch.bfloat16,
+                     device=cuda)
+    code = capi.DTYPE_F16 if dtype == "f16" else capi.DTYPE_BF16
+    capi.rows_to_half(H, 37, 90, 100, code, out, 96, d_absmax=mx, target=16384.0)
+    vol = H[:, :90].clone()
+    capi.volume_scale(vol, vol.numel(), d_absmax=mx, target=16384.0)
+    torch.cuda.synchronize()
+    assert float(mx) == 2.5e5
+    inv = 1.0 / torch.tensor(2.5e5 / 16384.0, dtype=torch.float32)
+    ref = (H[:, :90].cpu() * inv).to(out.dtype)
+    assert torch.equal(out[:, :90].cpu(), ref)
+    assert torch.all(out[:, 90:] == 0)
+    assert torch.allclose(vol, H[:, :90] * (2.5e5 / 16384.0), rtol=1e-6)
+
+
 def test_block_max_and_upsample(cuda):
     import torch
     import torch.nn.functional as F
@@ -328,8 +352,8 @@ def test_octree_pipeline_limits(cuda):
     assert not rec.computed_mask().any()
     fill = torch.empty_like(dense)
     capi.upsample_trilinear(rec.coarse, geo.coarse, fill, geo.fine, rec.stream)
+    rec._unscale(fill)
     rec.stream.synchronize()
-    torch.cuda.synchronize()
     assert torch.equal(out2, fill)
     rec.close()
 
@@ -345,3 +369,27 @@ def test_cnn_training_reduces_loss(cuda):
     hist = octree.train(model, coarse, bnorm, dims, epochs=40, batch=4, lr=5e-3, tau=0.7,
                         log=None)
     assert hist[-1] < 0.5 * hist[0], hist
+
+
+def test_trained_model_full_size_recall(cuda):
+    """The committed CNN on two held-out full-size octree_256 scenes: >= 99% of the
+    occupied voxels are backprojected at full resolution, from < 15% of the blocks, and
+    those voxels equal the dense pass."""
+    import torch
+
+    model, state = octree.OccupancyCNN.load(cuda)
+    geo = octree.OctreeGeometry.of("octree_256")
+    rec = octree.Reconstructor(geo, cuda)
+    lo = octree.logit(float(state["p_lo"]))
+    for seed in (3_000_001, 3_000_002):
+        rec.render(*octree.scene(geo, seed))
+        dense = rec.dense().clone()
+        out = rec.reconstruct(model, lo)
+        rec.stream.synchronize()
+        out = out.clone()
+        comp = rec.computed_mask()
+        m = octree.metrics(out, dense, comp, rec.occupied_voxels(dense))
+        assert m["recall"] >= 0.99, m
+        assert m["computed_fraction"] < 0.15, m
+        assert torch.equal(out[comp], dense[comp])
+    rec.close()
