@@ -173,7 +173,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_cnn_adam": (C.c_int, [_P, _P, _P, _P, C.c_uint64, C.c_float, C.c_float, C.c_float,
                                 C.c_float, C.c_uint32, _P]),
     "bpgb_cnn_normalize": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
-    "bpgb_cnn_features": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
+    "bpgb_cnn_features": (C.c_int, [_P, _U32, C.c_uint32, _P, _P, _P]),
 }
 
 _lib = None
@@ -641,9 +641,9 @@ def laplacian7(d_volume, voxels_per_side, d_out, stream=None) -> None:
                                 _stream_ptr(stream)), "bpgb_laplacian7")
 
 
-def cnn_features(d_coarse, dims, batch: int, d_X, stream=None) -> None:
+def cnn_features(d_coarse, dims, batch: int, d_X, d_scratch=None, stream=None) -> None:
     check(lib().bpgb_cnn_features(_ptr(d_coarse), u32ptr(_dims(dims)), int(batch), _ptr(d_X),
-                                  _stream_ptr(stream)), "bpgb_cnn_features")
+                                  _ptr(d_scratch), _stream_ptr(stream)), "bpgb_cnn_features")
 
 
 def rows_absmax(d_H, rows: int, T: int, pitch: int, d_max, stream=None) -> None:

@@ -95,6 +95,9 @@ struct FastArgs {
     // i < *tile_count; null = every tile of the volume
     const uint32_t *tile_list;
     const uint32_t *tile_count;
+    // tile-list launches with pair splits: partial sums are stored per list slot and
+    // split at tile-local voxel offsets (slot-major, then split, then voxel)
+    uint32_t tile_local;
 };
 
 struct TileGeo {
@@ -565,7 +568,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         for (int p = 0; p < NP; p++) acc[p].finish(comp[p]);
     }
     const float scale = a.splits > 1 ? 1.0f : a.out_scale;
-    const uint64_t part_off = a.splits > 1 ? (uint64_t)split * a.nvox : 0;
+    const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+    const uint64_t part_off = a.splits > 1 ? (uint64_t)split * (a.tile_local ? tvox : a.nvox) : 0;
 #pragma unroll
     for (int p = 0; p < NP; p++) {
 #pragma unroll
@@ -573,8 +577,14 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             const uint32_t kv = bk + (2 * p + w) * kstep;
             const uint32_t x = a.kax == 0 ? kv : bx, y = a.kax == 1 ? kv : by,
                            z = a.kax == 2 ? kv : bz;
-            if (x < a.n[0] && y < a.n[1] && z < a.n[2])
-                acc[p].store(out, part_off + ((uint64_t)x * a.n[1] + y) * a.n[2] + z, w, scale);
+            if (x < a.n[0] && y < a.n[1] && z < a.n[2]) {
+                const uint64_t idx =
+                    a.tile_local
+                        ? ((uint64_t)(x - g.org[0]) * a.tdim[1] + (y - g.org[1])) * a.tdim[2] +
+                              (z - g.org[2])
+                        : ((uint64_t)x * a.n[1] + y) * a.n[2] + z;
+                acc[p].store(out, part_off + idx, w, scale);
+            }
         }
     }
     return true;
@@ -605,11 +615,18 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     __shared__ int abort_flag;
     const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
     uint32_t tile = (uint32_t)(blockIdx.x % ntiles), split = (uint32_t)(blockIdx.x / ntiles);
+    void *dst = out;
     if (a.tile_list) {  // whole-CTA exits before any barrier is initialised
-        if (blockIdx.x >= *a.tile_count) return;
-        tile = a.tile_list[blockIdx.x];
-        split = 0;
+        const uint32_t slot = blockIdx.x / a.splits;
+        if (slot >= *a.tile_count) return;
+        tile = a.tile_list[slot];
+        split = blockIdx.x % a.splits;
         if (tile >= ntiles) return;
+        if (a.tile_local) {
+            constexpr uint32_t kOutEsz = Pair<HT>::kEsz == 8 ? 8 : 4;
+            const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+            dst = (unsigned char *)out + (uint64_t)slot * a.splits * tvox * kOutEsz;
+        }
     }
     PipeShared sh;
     sh.smem_raw = smem_raw;
@@ -628,7 +645,7 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     }
     __syncthreads();
     uint64_t step = 0;
-    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, out, diag, tile, split, 0,
+    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, dst, diag, tile, split, 0,
                                              step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
@@ -651,6 +668,46 @@ __global__ void reduce_splits_kernel(const float *__restrict__ partial, float *_
         }
         if (KAHAN) s -= c;
         out[i] = s * scale;
+    }
+}
+
+// Tile-list form of reduce_splits_kernel: slot s < *count holds tile list[s]; the
+// partial sums of its splits (slot-major, then split, then tile-local voxel) are added in split order
+// with the same arithmetic, so a voxel equals the full-volume reduction bit for bit.
+template <bool COMPLEX, bool KAHAN>
+__global__ void reduce_tiles_kernel(const float *__restrict__ partial,
+                                    const uint32_t *__restrict__ list,
+                                    const uint32_t *__restrict__ count, uint32_t max_tiles,
+                                    const FastArgs a, float *__restrict__ out) {
+    constexpr int C = COMPLEX ? 2 : 1;
+    const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+    const uint64_t n = (uint64_t)max_tiles * tvox * C;
+    const uint32_t cnt = *count;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t slot = i / (tvox * C);
+        if (slot >= cnt) break;
+        const uint64_t r = i - slot * tvox * C;
+        const uint64_t local = r / C;
+        const uint32_t c = (uint32_t)(r - local * C);
+        const uint32_t tile = list[slot];
+        const uint32_t tz = tile % a.tiles[2], tx = (tile / a.tiles[2]) % a.tiles[0],
+                       ty = tile / (a.tiles[2] * a.tiles[0]);
+        const uint32_t lz = (uint32_t)(local % a.tdim[2]),
+                       ly = (uint32_t)((local / a.tdim[2]) % a.tdim[1]),
+                       lx = (uint32_t)(local / ((uint64_t)a.tdim[2] * a.tdim[1]));
+        const uint32_t x = tx * a.tdim[0] + lx, y = ty * a.tdim[1] + ly, z = tz * a.tdim[2] + lz;
+        if (x >= a.n[0] || y >= a.n[1] || z >= a.n[2]) continue;
+        float s = 0.0f, cmp = 0.0f;
+        for (uint32_t k = 0; k < a.splits; k++) {
+            const float v = partial[((slot * a.splits + k) * tvox + local) * C + c];
+            if (KAHAN)
+                kahan_add(s, cmp, v);
+            else
+                s += v;
+        }
+        if (KAHAN) s -= cmp;
+        out[(((uint64_t)x * a.n[1] + y) * a.n[2] + z) * C + c] = s * a.out_scale;
     }
 }
 
@@ -1058,8 +1115,12 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
         tab[fz.S + l] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)c);
     }
     const size_t tab_bytes = tab.size() * sizeof(float4);
+    // partial sums: [split][voxel] for full launches, [slot][split][tile voxel] for
+    // tile-list launches (tiles x tile voxels >= voxels)
     const size_t part_bytes =
-        splits > 1 ? (size_t)splits * a.nvox * (dt == BPGB_DTYPE_C64 ? 8 : 4) : 0;
+        splits > 1 ? (size_t)splits * ntiles * a.tdim[0] * a.tdim[1] * a.tdim[2] *
+                         (dt == BPGB_DTYPE_C64 ? 8 : 4)
+                   : 0;
     e = cudaMalloc(&fp->d_tables, tab_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess && part_bytes) e = cudaMalloc(&fp->d_partial, part_bytes);
@@ -1119,9 +1180,9 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     const FastArgs &a0 = fp->a;
     const uint64_t ntiles = (uint64_t)a0.tiles[0] * a0.tiles[1] * a0.tiles[2];
     if (!d_list || !d_count) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null tile list");
-    if (a0.splits != 1)
-        return set_error(BPGB_ERR_UNSUPPORTED, "tile-list launches need a plan with pair_splits = 1");
     if (max_tiles == 0) return BPGB_OK;
+    if ((uint64_t)max_tiles * a0.splits >= (1ull << 31))
+        return set_error(BPGB_ERR_UNSUPPORTED, "tile list x pair splits too large for one grid");
     if (max_tiles > ntiles)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "max_tiles exceeds the plan's tile count");
     if (((uintptr_t)d_H) % 16) return set_error(BPGB_ERR_INVALID_ARGUMENT, "H must be 16-byte aligned");
@@ -1131,13 +1192,35 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     FastArgs a = a0;
     a.tile_list = d_list;
     a.tile_count = d_count;
+    a.tile_local = a.splits > 1 ? 1 : 0;
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
+    void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
     void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
-    void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&d_out,
+    void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&a};
-    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(max_tiles), dim3(fp->threads), args, fp->smem, stream));
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(max_tiles * a.splits), dim3(fp->threads), args,
+                                   fp->smem, stream));
     count_launches(1);
+    if (a.splits > 1) {
+        const bool cplx = fp->dtype == BPGB_DTYPE_C64;
+        const uint64_t n = (uint64_t)max_tiles * a.tdim[0] * a.tdim[1] * a.tdim[2] * (cplx ? 2 : 1);
+        const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8);
+        float *o = (float *)d_out;
+        if (cplx) {
+            if (fp->kahan)
+                reduce_tiles_kernel<true, true><<<blocks, 256, 0, stream>>>(fp->d_partial, d_list, d_count, max_tiles, a, o);
+            else
+                reduce_tiles_kernel<true, false><<<blocks, 256, 0, stream>>>(fp->d_partial, d_list, d_count, max_tiles, a, o);
+        } else {
+            if (fp->kahan)
+                reduce_tiles_kernel<false, true><<<blocks, 256, 0, stream>>>(fp->d_partial, d_list, d_count, max_tiles, a, o);
+            else
+                reduce_tiles_kernel<false, false><<<blocks, 256, 0, stream>>>(fp->d_partial, d_list, d_count, max_tiles, a, o);
+        }
+        count_launches(1);
+        BPGB_CUDA_TRY(cudaGetLastError());
+    }
     return BPGB_OK;
 }
 

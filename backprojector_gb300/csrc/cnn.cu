@@ -387,6 +387,56 @@ __global__ void features_kernel(const float *__restrict__ coarse, Geo g,
     }
 }
 
+// Grid-wide form of features_kernel: pass 1 folds each sample's max(c, 0) and max |F|
+// into scratch[2 s], scratch[2 s + 1] (float bits compare as unsigned for values >= 0),
+// pass 2 writes both channels.
+__device__ __forceinline__ float lap7(const float *c, const Geo &g, uint64_t r) {
+    const uint32_t z = (uint32_t)(r % g.n2), y = (uint32_t)((r / g.n2) % g.n1),
+                   x = (uint32_t)(r / ((uint64_t)g.n2 * g.n1));
+    const float v = c[r];
+    float s = 0.0f;
+    if (x > 0) s += v - c[r - (uint64_t)g.n1 * g.n2];
+    if (x + 1 < g.n0) s += v - c[r + (uint64_t)g.n1 * g.n2];
+    if (y > 0) s += v - c[r - g.n2];
+    if (y + 1 < g.n1) s += v - c[r + g.n2];
+    if (z > 0) s += v - c[r - 1];
+    if (z + 1 < g.n2) s += v - c[r + 1];
+    return s;
+}
+
+__global__ void features_max_kernel(const float *__restrict__ coarse, Geo g,
+                                    unsigned int *__restrict__ scratch) {
+    const float *c = coarse + blockIdx.y * g.vox;
+    float m0 = 0.0f, m1 = 0.0f;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < g.vox;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        m0 = fmaxf(m0, c[i]);
+        m1 = fmaxf(m1, fabsf(lap7(c, g, i)));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+        m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&scratch[2 * blockIdx.y], __float_as_uint(m0));
+        atomicMax(&scratch[2 * blockIdx.y + 1], __float_as_uint(m1));
+    }
+}
+
+__global__ void features_write_kernel(const float *__restrict__ coarse, Geo g,
+                                      const unsigned int *__restrict__ scratch,
+                                      __nv_bfloat16 *__restrict__ X) {
+    const float *c = coarse + blockIdx.y * g.vox;
+    const float mx0 = __uint_as_float(scratch[2 * blockIdx.y]);
+    const float mx1 = __uint_as_float(scratch[2 * blockIdx.y + 1]);
+    const float i0 = mx0 > 0.0f ? 1.0f / mx0 : 0.0f, i1 = mx1 > 0.0f ? 1.0f / mx1 : 0.0f;
+    __nv_bfloat16 *x = X + blockIdx.y * g.vox * 2;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < g.vox;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        *reinterpret_cast<__nv_bfloat162 *>(x + 2 * i) =
+            __floats2bfloat162_rn(c[i] * i0, lap7(c, g, i) * i1);
+}
+
 template <int CIN, int NP>
 int launch_fwd(const void *X, uint32_t xs, const Geo &g, const void *Wt, int relu,
                const void *mask, uint32_t ms, void *Y, float *Yf, cudaStream_t s) {
@@ -540,13 +590,24 @@ int bpgb_cnn_normalize(const float *d_coarse, const uint32_t *dims, uint32_t bat
 }
 
 int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
-                      void *stream) {
+                      float *d_scratch, void *stream) {
     clear_error();
     Geo g;
-    if (!d_coarse || !d_X || !geo_of(dims, batch, &g))
+    if (!d_coarse || !d_X || !geo_of(dims, batch, &g) || ((uintptr_t)d_X) % 4)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad features arguments");
-    features_kernel<<<batch, 256, 0, (cudaStream_t)stream>>>(d_coarse, g, (__nv_bfloat16 *)d_X);
-    count_launches(1);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!d_scratch || batch > 65535) {
+        features_kernel<<<batch, 256, 0, s>>>(d_coarse, g, (__nv_bfloat16 *)d_X);
+        count_launches(1);
+    } else {
+        BPGB_CUDA_TRY(cudaMemsetAsync(d_scratch, 0, 2 * sizeof(float) * batch, s));
+        const uint64_t per = (g.vox + 255) / 256;
+        const dim3 grid((unsigned)(per < 64 ? per : 64), batch);
+        features_max_kernel<<<grid, 256, 0, s>>>(d_coarse, g, (unsigned int *)d_scratch);
+        features_write_kernel<<<grid, 256, 0, s>>>(d_coarse, g, (const unsigned int *)d_scratch,
+                                                   (__nv_bfloat16 *)d_X);
+        count_launches(2);
+    }
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
 }

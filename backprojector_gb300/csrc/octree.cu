@@ -106,39 +106,35 @@ __global__ void block_max_kernel(const float *__restrict__ vol, uint32_t n0, uin
 }
 
 // fine[i, j, k] = trilinear sample of coarse at (i (c0-1)/(f0-1), ...): both grids span
-// the same box with the reference's spacing size / (n - 1).
+// the same box with the reference's spacing size / (n - 1).  One CTA per fine (i, j) line:
+// the four coarse z-lines around it are blended in x and y once into shared memory, then
+// the threads interpolate along z and write the line with coalesced stores.
 __global__ void upsample_kernel(const float *__restrict__ coarse, uint32_t c0, uint32_t c1,
                                 uint32_t c2, float *__restrict__ fine, uint32_t f0, uint32_t f1,
                                 uint32_t f2) {
-    const uint64_t n = (uint64_t)f0 * f1 * f2;
+    extern __shared__ float line[];  // c2 floats
+    const uint32_t j = blockIdx.x, i = blockIdx.y;
     const float s0 = f0 > 1 ? (float)(c0 - 1) / (float)(f0 - 1) : 0.0f;
     const float s1 = f1 > 1 ? (float)(c1 - 1) / (float)(f1 - 1) : 0.0f;
     const float s2 = f2 > 1 ? (float)(c2 - 1) / (float)(f2 - 1) : 0.0f;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-         v += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t k = (uint32_t)(v % f2), j = (uint32_t)((v / f2) % f1),
-                       i = (uint32_t)(v / ((uint64_t)f2 * f1));
-        const float u[3] = {i * s0, j * s1, k * s2};
-        const uint32_t cn[3] = {c0, c1, c2};
-        uint32_t lo[3], hi[3];
-        float w[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++) {
-            const float fl = floorf(u[a]);
-            lo[a] = min((uint32_t)fl, cn[a] - 1);
-            hi[a] = min(lo[a] + 1, cn[a] - 1);
-            w[a] = u[a] - fl;
-        }
-        auto at = [&](uint32_t x, uint32_t y, uint32_t z) {
-            return coarse[((uint64_t)x * c1 + y) * c2 + z];
-        };
-        const float c00 = at(lo[0], lo[1], lo[2]) * (1 - w[2]) + at(lo[0], lo[1], hi[2]) * w[2];
-        const float c01 = at(lo[0], hi[1], lo[2]) * (1 - w[2]) + at(lo[0], hi[1], hi[2]) * w[2];
-        const float c10 = at(hi[0], lo[1], lo[2]) * (1 - w[2]) + at(hi[0], lo[1], hi[2]) * w[2];
-        const float c11 = at(hi[0], hi[1], lo[2]) * (1 - w[2]) + at(hi[0], hi[1], hi[2]) * w[2];
-        const float c0v = c00 * (1 - w[1]) + c01 * w[1];
-        const float c1v = c10 * (1 - w[1]) + c11 * w[1];
-        fine[v] = c0v * (1 - w[0]) + c1v * w[0];
+    const float u0 = i * s0, u1 = j * s1;
+    const float fl0 = floorf(u0), fl1 = floorf(u1);
+    const uint32_t x0 = min((uint32_t)fl0, c0 - 1), x1 = min(x0 + 1, c0 - 1);
+    const uint32_t y0 = min((uint32_t)fl1, c1 - 1), y1 = min(y0 + 1, c1 - 1);
+    const float w0 = u0 - fl0, w1 = u1 - fl1;
+    for (uint32_t z = threadIdx.x; z < c2; z += blockDim.x) {
+        auto at = [&](uint32_t x, uint32_t y) { return coarse[((uint64_t)x * c1 + y) * c2 + z]; };
+        const float a0 = at(x0, y0) * (1 - w1) + at(x0, y1) * w1;
+        const float a1 = at(x1, y0) * (1 - w1) + at(x1, y1) * w1;
+        line[z] = a0 * (1 - w0) + a1 * w0;
+    }
+    __syncthreads();
+    float *out = fine + ((uint64_t)i * f1 + j) * f2;
+    for (uint32_t k = threadIdx.x; k < f2; k += blockDim.x) {
+        const float u2 = k * s2, fl2 = floorf(u2);
+        const uint32_t z0 = min((uint32_t)fl2, c2 - 1), z1 = min(z0 + 1, c2 - 1);
+        const float w2 = u2 - fl2;
+        out[k] = line[z0] * (1 - w2) + line[z1] * w2;
     }
 }
 
@@ -219,11 +215,12 @@ int bpgb_upsample_trilinear(const float *d_coarse, const uint32_t *coarse_dims, 
     for (int a = 0; a < 3; a++)
         if (!coarse_dims[a] || !fine_dims[a])
             return set_error(BPGB_ERR_INVALID_ARGUMENT, "empty grid");
-    const uint64_t n = (uint64_t)fine_dims[0] * fine_dims[1] * fine_dims[2];
-    const unsigned grid = (unsigned)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
-    upsample_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_coarse, coarse_dims[0], coarse_dims[1],
-                                                          coarse_dims[2], d_fine, fine_dims[0],
-                                                          fine_dims[1], fine_dims[2]);
+    if (fine_dims[0] > 65535 || fine_dims[1] > (1u << 31) - 1 || coarse_dims[2] > 12288)
+        return set_error(BPGB_ERR_UNSUPPORTED, "upsample grid too large");
+    const dim3 grid(fine_dims[1], fine_dims[0]);
+    upsample_kernel<<<grid, 256, coarse_dims[2] * sizeof(float), (cudaStream_t)stream>>>(
+        d_coarse, coarse_dims[0], coarse_dims[1], coarse_dims[2], d_fine, fine_dims[0],
+        fine_dims[1], fine_dims[2]);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;

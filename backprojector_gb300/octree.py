@@ -127,7 +127,8 @@ class OccupancyCNN:
         if self.in_channels == 1:
             capi.cnn_normalize(coarse, dims, batch, X, stream)
         else:
-            capi.cnn_features(coarse, dims, batch, X, stream)
+            scr = self._buf(f"feat{batch}", (2 * batch,), self.torch.float32)
+            capi.cnn_features(coarse, dims, batch, X, scr, stream)
         return X
 
     def forward(self, X0, dims, batch: int, logits=None, stream=None):
@@ -232,7 +233,7 @@ class Reconstructor:
     back at the end of each pass)."""
 
     def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = 10,
-                 h_dtype: int = capi.DTYPE_F16, **fine_opt):
+                 h_dtype: int = capi.DTYPE_F16, fine_splits: int = 4, **fine_opt):
         import torch
 
         self.torch = torch
@@ -255,7 +256,9 @@ class Reconstructor:
         # The fine plan serves both the dense reference (execute) and the block-sparse
         # pass (execute_tiles): FAST arithmetic is tile-relative, so one plan gives
         # bit-identical voxels in both.
-        opt = dict(algo=capi.ALGO_FAST, pair_splits=1, h_dtype=h_dtype)
+        # pair splits: a few hundred to a few thousand selected tiles fill 1-3 waves of
+        # CTAs; splitting each tile's pairs over 4 CTAs keeps the last wave short
+        opt = dict(algo=capi.ALGO_FAST, pair_splits=fine_splits, h_dtype=h_dtype)
         if fine_tile is not None:
             opt["tile"] = fine_tile
         opt.update(fine_opt)

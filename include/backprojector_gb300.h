@@ -156,11 +156,14 @@ int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_
                      const float *volume_zero_pos, const float *voxel_inc, float t0,
                      float deltaT, const bpgb_options *opt);
 int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *stream);
-/* Block-sparse form of bpgb_plan_execute (FAST plans with pair_splits = 1): computes
- * only the voxel tiles listed in device memory, d_tile_list[0 .. *d_tile_count), and
- * leaves every other voxel of d_volume untouched.  max_tiles bounds *d_tile_count and
- * sets the launch size, so the call reads no device value on the host and can be
- * captured in a CUDA graph.  Tile ids follow the plan's tile grid
+/* Block-sparse form of bpgb_plan_execute (FAST plans): computes only the voxel tiles
+ * listed in device memory, d_tile_list[0 .. *d_tile_count), and leaves every other voxel
+ * of d_volume untouched.  max_tiles bounds *d_tile_count and sets the launch size
+ * (max_tiles x pair_splits CTAs; those past the count exit at once), so the call reads
+ * no device value on the host and can be captured in a CUDA graph.  With pair_splits > 1
+ * each listed tile's pairs are split over that many CTAs and a second kernel adds the
+ * partial sums in split order, exactly as bpgb_plan_execute does, so the listed voxels
+ * equal the full execute's bit for bit.  Tile ids follow the plan's tile grid
  * (bpgb_plan_info.tile voxels per tile; id = (ty * tiles_x + tx) * tiles_z + tz). */
 int bpgb_plan_execute_tiles(bpgb_plan plan, const void *d_H, void *d_volume,
                             const uint32_t *d_tile_list, const uint32_t *d_tile_count,
@@ -333,9 +336,10 @@ int bpgb_cnn_normalize(const float *d_coarse, const uint32_t *dims, uint32_t bat
                        void *stream);
 /* Two input channels per voxel, d_X BF16 [batch * n0 n1 n2][2]: the sample divided by
  * its maximum, and its negated 7-point Laplacian (as bpgb_laplacian7) divided by its
- * largest magnitude. */
+ * largest magnitude.  d_scratch (2 x batch floats, overwritten) lets the maxima be
+ * reduced across the whole GPU; NULL reduces each sample in one CTA (slower). */
 int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
-                      void *stream);
+                      float *d_scratch, void *stream);
 
 /* ---- autotuner -------------------------------------------------------------------
  * No counterpart in the reference (its launch shape is fixed: 16^3 voxels per launch,

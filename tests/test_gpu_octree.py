@@ -181,15 +181,17 @@ def test_device_renderer_matches_host_renderer(cuda):
     assert torch.equal(H, H2)
 
 
-def test_cnn_features_vs_torch(cuda):
+@pytest.mark.parametrize("grid_wide", [False, True])
+def test_cnn_features_vs_torch(cuda, grid_wide):
     import torch
     import torch.nn.functional as F
 
     g = torch.Generator().manual_seed(9)
-    dims, batch = (6, 7, 5), 2
+    dims, batch = (6, 7, 5) if not grid_wide else (32, 32, 32), 2
     coarse = torch.rand((batch, *dims), generator=g)
     X = torch.empty((batch * int(np.prod(dims)) * 2,), dtype=torch.bfloat16, device=cuda)
-    capi.cnn_features(coarse.to(cuda), dims, batch, X)
+    scr = torch.full((2 * batch,), 7.0, device=cuda) if grid_wide else None
+    capi.cnn_features(coarse.to(cuda), dims, batch, X, scr)
     torch.cuda.synchronize()
     got = X.float().cpu().reshape(batch, *dims, 2)
     k = torch.zeros((1, 1, 3, 3, 3))
@@ -284,8 +286,8 @@ def test_small_tile_presets_vs_oracle(cuda, tile):
     assert oracle.rel_l2(dV.cpu().numpy(), ref) < 5e-3
 
 
-@pytest.mark.parametrize("tile", [0, 10])
-def test_tile_list_execution_matches_dense(cuda, tile):
+@pytest.mark.parametrize("tile,splits", [(0, 1), (10, 1), (10, 2), (11, 3), (0, 4)])
+def test_tile_list_execution_matches_dense(cuda, tile, splits):
     import torch
 
     c = synthetic.make_capture("octree_256", seed=6, small=True)
@@ -293,9 +295,10 @@ def test_tile_list_execution_matches_dense(cuda, tile):
     N = tuple(int(v) for v in c.voxels_per_side)
     dense = torch.empty(N, device=cuda)
     with capi.Plan(c.pairs, c.T, N, c.zero, c.inc, c.t0, c.deltaT, algo=capi.ALGO_FAST,
-                   tile=tile, pair_splits=1) as p:
+                   tile=tile, pair_splits=splits) as p:
         p.execute(dH, dense)
         info = p.info()
+        assert info["pair_splits"] == splits
         td = info["tile"]
         nt = [-(-n // t) for n, t in zip(N, td)]
         ntiles = int(np.prod(nt))
