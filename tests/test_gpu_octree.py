@@ -395,4 +395,16 @@ def test_trained_model_full_size_recall(cuda):
         assert m["recall"] >= 0.99, m
         assert m["computed_fraction"] < 0.15, m
         assert torch.equal(out[comp], dense[comp])
+        # occupied voxels of the octree volume against the FP64 oracle (256-voxel sample)
+        occ = (rec.occupied_voxels(dense) & comp).reshape(-1)
+        ids_all = torch.nonzero(occ).reshape(-1).cpu().numpy()
+        ids = np.sort(np.random.default_rng(seed).choice(ids_all, size=min(256, len(ids_all)),
+                                                         replace=False))
+        ref = oracle.bp_gpu_f64(rec.H.cpu().numpy(), geo.pairs, geo.fine, geo.zero, geo.inc_fine,
+                                geo.t0, geo.deltaT, voxels=ids)
+        got = out.reshape(-1)[torch.from_numpy(ids).to(cuda)].double().cpu().numpy()
+        err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        print(f"\n[octree_256 seed {seed}] recall {m['recall']:.5f} computed "
+              f"{m['computed_fraction']:.4f} occupied-voxel rel-L2 vs FP64 oracle {err:.2e}")
+        assert err <= 1e-3
     rec.close()

@@ -426,3 +426,32 @@ def test_nlosbpy_phasor_matches_oracle_pipeline(cuda):
     ref = oracle.bp_gpu_c64(Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, float(ct0), c.deltaT)
     assert vol.dtype == np.complex64
     assert oracle.rel_l2(vol, ref) < 5e-3
+
+
+def test_reference_kernel_speed_on_256_capture(cuda):
+    """The reference's own kernel (built from its sources, its launcher's policy) against
+    the FAST plan on the 256^3 capture, on the same GPU; prints both rates."""
+    import torch
+
+    if not oracle.REF_LIB.exists():
+        pytest.skip("reference kernel not built (reference sources absent at build time)")
+    c = synthetic.make_capture("octree_256", seed=0)
+    _, block, ref_ms = oracle.reference_gpu(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc,
+                                            c.t0, c.deltaT)
+    dH = torch.from_numpy(c.H).to(cuda)
+    dV = torch.empty(tuple(int(v) for v in c.voxels_per_side), device=cuda)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST) as p:
+        p.execute(dH, dV)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(3):
+            p.execute(dH, dV)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+    print(f"\n[octree_256 dense] reference kernel (block {block}) {ref_ms:.1f} ms = "
+          f"{c.updates / ref_ms * 1e3:.3e} updates/s; FAST {ms:.2f} ms = "
+          f"{c.updates / ms * 1e3:.3e} updates/s; ratio {ref_ms / ms:.1f}")
+    assert ms * 10 < ref_ms
