@@ -35,7 +35,8 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 
 CU_SOURCES = ["bp_exact.cu", "bp_fast.cu", "phasor.cu", "geometry.cu", "diag.cu", "octree.cu", "cnn.cu", "rows.cu"]
-CPP_SOURCES = ["capi.cpp", "capture.cpp", "shim.cpp", "synth.cpp", "tune.cpp"]
+CPP_SOURCES = ["capi.cpp", "capture.cpp", "shim.cpp", "synth.cpp", "tune.cpp", "npy.cpp",
+               "octree_host.cpp"]
 
 LIB_PATH = LIBDIR / "libbpgb300.so"
 ORACLE_LIB = ORACLE / "_build" / "liboracle.so"

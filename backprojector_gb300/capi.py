@@ -82,6 +82,18 @@ class TuneReport(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class OctreeInfo(C.Structure):
+    _fields_ = [("fine", C.c_uint32 * 3), ("coarse", C.c_uint32 * 3), ("tile", C.c_uint32 * 3),
+                ("tiles", C.c_uint32), ("in_channels", C.c_uint32), ("pair_splits", C.c_uint32),
+                ("h_dtype", C.c_int32), ("p_lo", C.c_float), ("scratch_bytes", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        for k in ("fine", "coarse", "tile"):
+            d[k] = list(d[k])
+        return d
+
+
 class BackprojectorError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(message)
@@ -157,6 +169,13 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_block_max": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
     "bpgb_upsample_trilinear": (C.c_int, [_P, _U32, _P, _U32, _P]),
     "bpgb_laplacian7": (C.c_int, [_P, _U32, _P, _P]),
+    "bpgb_octree_create": (C.c_int, [C.POINTER(_P), _P, C.c_uint64, C.c_uint32, _U32, _F, _F,
+                                     C.c_float, C.c_float, C.c_char_p, C.c_float,
+                                     C.POINTER(Options)]),
+    "bpgb_octree_reconstruct": (C.c_int, [_P, _P, _P, _P]),
+    "bpgb_octree_selected": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "bpgb_octree_get_info": (C.c_int, [_P, C.POINTER(OctreeInfo)]),
+    "bpgb_octree_destroy": (C.c_int, [_P]),
     "bpgb_rows_absmax": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, _P, _P]),
     "bpgb_rows_to_half": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P,
                                     C.c_float, C.c_int, _P, C.c_uint32, _P]),
@@ -662,3 +681,52 @@ def volume_scale(d_volume, n: int, scale: float = 1.0, d_absmax=None, target: fl
                  stream=None) -> None:
     check(lib().bpgb_volume_scale(_ptr(d_volume), int(n), float(scale), _ptr(d_absmax),
                                   float(target), _stream_ptr(stream)), "bpgb_volume_scale")
+
+
+class NativeOctree:
+    """bpgb_octree: the learned-octree reconstruction as one native object (weights from
+    an .npz written by backprojector_gb300.octree_train)."""
+
+    def __init__(self, pairs, T: int, voxels_per_side, zero, inc, t0: float, deltaT: float,
+                 weights, p_lo: float = 0.0, **opt):
+        self._pairs = np.ascontiguousarray(pairs, dtype=PAIR_DTYPE)
+        n = np.asarray([int(v) for v in voxels_per_side], np.uint32)
+        self.n = tuple(int(v) for v in n)
+        self.opt = options(**opt)
+        h = C.c_void_p()
+        check(lib().bpgb_octree_create(C.byref(h), vptr(self._pairs), len(self._pairs), int(T),
+                                       u32ptr(n), fptr(f32(zero)), fptr(f32(inc)), float(t0),
+                                       float(deltaT), str(weights).encode(), float(p_lo),
+                                       C.byref(self.opt)), "bpgb_octree_create")
+        self.handle = h
+
+    def reconstruct(self, d_H, d_volume, stream=None) -> None:
+        check(lib().bpgb_octree_reconstruct(self.handle, _ptr(d_H), _ptr(d_volume),
+                                            _stream_ptr(stream)), "bpgb_octree_reconstruct")
+
+    def selected(self) -> int:
+        v = C.c_uint32()
+        check(lib().bpgb_octree_selected(self.handle, C.byref(v)), "bpgb_octree_selected")
+        return int(v.value)
+
+    def info(self) -> dict:
+        i = OctreeInfo()
+        check(lib().bpgb_octree_get_info(self.handle, C.byref(i)), "bpgb_octree_get_info")
+        return i.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().bpgb_octree_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

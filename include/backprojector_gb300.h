@@ -341,6 +341,41 @@ int bpgb_cnn_normalize(const float *d_coarse, const uint32_t *dims, uint32_t bat
 int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
                       float *d_scratch, void *stream);
 
+/* ---- learned octree as one native object --------------------------------------------
+ * Replaces the reference's octree entry (call_cuda_octree_backprojection,
+ * backproject_cuda.hpp:30-39, whose GPU implementation backproject_cuda.cu:503-669 prints
+ * "NOT WORKING YET"; the CPU threshold octree backproject.hpp:264-335).  Per reconstruct,
+ * on `stream`: (FP16 mode) scale and store the rows as FP16 on the device; the FAST pass
+ * on the 8x coarser grid over the same box; the occupancy CNN (weights from an .npz written
+ * by backprojector_gb300.octree_train: w0..w3 [kp][cout] FP32, in_channels, p_lo); the
+ * trilinear fill of the whole volume; a full-resolution pass over the 8^3 blocks scoring
+ * p >= p_lo (tile list, pair splits); the FP16 scale undone.  voxels_per_side must be
+ * multiples of 8 (>= 16); d_H holds FP32 rows of pitch T.  opt: h_dtype F32 or F16
+ * (default F16), tile (-1: 8^3 tiles), pair_splits (0: 4), chunk, stages.  p_lo <= 0
+ * takes the weights file's.  Buffers are allocated at create; reconstruct allocates
+ * nothing and reads no device value on the host. */
+typedef struct bpgb_octree_info {
+    uint32_t fine[3], coarse[3], tile[3];
+    uint32_t tiles;        /* fine tiles in the volume */
+    uint32_t in_channels;  /* CNN input channels (1 or 2) */
+    uint32_t pair_splits;
+    int32_t h_dtype;
+    float p_lo;
+    uint64_t scratch_bytes; /* device memory held */
+} bpgb_octree_info;
+
+typedef struct bpgb_octree_s *bpgb_octree;
+
+int bpgb_octree_create(bpgb_octree *octree, const bpgb_pair *host_pairs, uint64_t num_pairs,
+                       uint32_t T, const uint32_t *voxels_per_side, const float *volume_zero_pos,
+                       const float *voxel_inc, float t0, float deltaT, const char *weights_path,
+                       float p_lo, const bpgb_options *opt);
+int bpgb_octree_reconstruct(bpgb_octree octree, const float *d_H, float *d_volume, void *stream);
+/* Synchronises the last reconstruct's stream; *tiles = fine tiles it computed. */
+int bpgb_octree_selected(bpgb_octree octree, uint32_t *tiles);
+int bpgb_octree_get_info(bpgb_octree octree, bpgb_octree_info *info);
+int bpgb_octree_destroy(bpgb_octree octree);
+
 /* ---- autotuner -------------------------------------------------------------------
  * No counterpart in the reference (its launch shape is fixed: 16^3 voxels per launch,
  * the largest power-of-two block not above the pair count).  Times FAST configurations

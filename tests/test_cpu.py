@@ -193,3 +193,25 @@ def test_tune_cache_file_round_trip(tmp_path):
     assert capi.tune_cache_size() == 2
     capi.tune_cache_clear()
     assert capi.tune_cache_size() == 0
+
+
+def test_native_octree_weights_file_errors(tmp_path):
+    """bpgb_octree_create reads its weights with the library's own .npz reader: missing,
+    malformed, compressed and mis-shaped files are rejected before any device work."""
+    c = synthetic.make_capture("octree_256", small=True, render=False)
+    args = (c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    cases = {"missing.npz": "cannot open"}
+    (tmp_path / "junk.npz").write_bytes(b"not a zip archive at all, just some bytes")
+    cases["junk.npz"] = "end-of-directory"
+    np.savez_compressed(tmp_path / "packed.npz", w0=np.zeros((32, 16), np.float32))
+    cases["packed.npz"] = "compressed"
+    np.savez(tmp_path / "shape.npz", w0=np.zeros((3, 3), np.float32), in_channels=np.int64(2),
+             p_lo=np.float64(0.1))
+    for name, msg in cases.items():
+        with pytest.raises(capi.BackprojectorError) as e:
+            capi.NativeOctree(*args, tmp_path / name)
+        assert e.value.status == capi.ERR_INVALID_ARGUMENT and msg in str(e.value), str(e.value)
+    # a well-formed file gets past the reader (then needs a device for its plans)
+    with pytest.raises(capi.BackprojectorError) as e:
+        capi.NativeOctree(*args, tmp_path / "shape.npz")
+    assert "cannot open" not in str(e.value) and "zip" not in str(e.value)
