@@ -154,6 +154,20 @@ def build_reference(verbose: bool = False) -> Path | None:
     return REF_LIB
 
 
+CLI_PATH = LIBDIR / "bpgb_backprojector"
+
+
+def build_cli(verbose: bool = False) -> Path:
+    """The command-line tool (csrc/cli.cpp) linked against the library."""
+    src = CSRC / "cli.cpp"
+    if _stale(CLI_PATH, [src, LIB_PATH, *_headers()]):
+        _run(["g++", "-std=c++17", "-O2", f"-I{INCLUDE}", f"-I{CSRC}", str(src), "-o",
+              str(CLI_PATH), f"-L{LIBDIR}", "-lbpgb300", "-Wl,-rpath,$ORIGIN"])
+    if verbose:
+        print(f"built {CLI_PATH}")
+    return CLI_PATH
+
+
 def build_all(verbose: bool = False) -> None:
     if shutil.which(NVCC) is None and not Path(NVCC).exists():
         raise RuntimeError("nvcc not found; set CUDA_HOME")
@@ -165,6 +179,7 @@ def build_all(verbose: bool = False) -> None:
         f_orc.result()
         f_ref.result()
     build_python_module(verbose)
+    build_cli(verbose)
 
 
 if __name__ == "__main__":

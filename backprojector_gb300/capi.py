@@ -173,6 +173,7 @@ SIGNATURES: dict[str, tuple] = {
                                      C.c_float, C.c_float, C.c_char_p, C.c_float,
                                      C.POINTER(Options)]),
     "bpgb_octree_reconstruct": (C.c_int, [_P, _P, _P, _P]),
+    "bpgb_octree_reconstruct_host": (C.c_int, [_P, _P, _P]),
     "bpgb_octree_selected": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "bpgb_octree_get_info": (C.c_int, [_P, C.POINTER(OctreeInfo)]),
     "bpgb_octree_destroy": (C.c_int, [_P]),
@@ -703,6 +704,13 @@ class NativeOctree:
     def reconstruct(self, d_H, d_volume, stream=None) -> None:
         check(lib().bpgb_octree_reconstruct(self.handle, _ptr(d_H), _ptr(d_volume),
                                             _stream_ptr(stream)), "bpgb_octree_reconstruct")
+
+    def reconstruct_host(self, H: np.ndarray) -> np.ndarray:
+        Hc = np.ascontiguousarray(H, dtype=np.float32)
+        out = np.empty(self.n, np.float32)
+        check(lib().bpgb_octree_reconstruct_host(self.handle, Hc.ctypes.data, out.ctypes.data),
+              "bpgb_octree_reconstruct_host")
+        return out
 
     def selected(self) -> int:
         v = C.c_uint32()

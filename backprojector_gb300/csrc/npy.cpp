@@ -219,7 +219,10 @@ bool npz_load(const std::string &path, std::map<std::string, NpyArray> *out, std
         if (csize != usize || data + csize > n) return fail(name + ": bad member size");
         NpyArray a;
         std::string w;
-        if (!npy_parse(&buf[data], (size_t)csize, &a, &w)) return fail(name + ": " + w);
+        if (!npy_parse(&buf[data], (size_t)csize, &a, &w)) {
+            if (w.compare(0, 17, "unsupported dtype") == 0) continue;  // e.g. text members
+            return fail(name + ": " + w);
+        }
         if (name.size() > 4 && name.compare(name.size() - 4, 4, ".npy") == 0)
             name = name.substr(0, name.size() - 4);
         (*out)[name] = std::move(a);

@@ -24,7 +24,8 @@ struct NpyArray {
 // Parses one .npy image; false with *why on a format it does not handle.
 bool npy_parse(const unsigned char *data, size_t size, NpyArray *out, std::string *why);
 bool npy_load(const std::string &path, NpyArray *out, std::string *why);
-// Every member of an uncompressed .npz ("name.npy" entries, keys without ".npy").
+// Every member of an uncompressed .npz ("name.npy" entries, keys without ".npy");
+// members of other element types (text, objects) are skipped.
 bool npz_load(const std::string &path, std::map<std::string, NpyArray> *out, std::string *why);
 // Writes a float32 C-ordered .npy (version 1.0 header).
 bool npy_save_f32(const std::string &path, const float *data, const std::vector<uint64_t> &shape,

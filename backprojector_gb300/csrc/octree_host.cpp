@@ -44,6 +44,7 @@ struct bpgb_octree_s {
     uint32_t *tile_list = nullptr, *tile_count = nullptr;
     uint64_t scratch = 0;
     cudaStream_t last = nullptr;
+    float *io_H = nullptr, *io_vol = nullptr;  // device copies for the host-buffer call
 };
 
 namespace {
@@ -62,6 +63,8 @@ void octree_free(bpgb_octree_s *o) {
     for (void *p : o->Y) cudaFree(p);
     cudaFree(o->tile_list);
     cudaFree(o->tile_count);
+    cudaFree(o->io_H);
+    cudaFree(o->io_vol);
     delete o;
 }
 
@@ -79,6 +82,7 @@ int bpgb_octree_create(bpgb_octree *out, const bpgb_pair *pairs, uint64_t num_pa
     *out = nullptr;
     bpgb_options o;
     bpgb_options_default(&o);
+    o.h_dtype = BPGB_DTYPE_F16;  // NULL opt: FP16 rows
     if (opt) o = *opt;
     if (o.h_dtype != BPGB_DTYPE_F32 && o.h_dtype != BPGB_DTYPE_F16)
         return set_error(BPGB_ERR_UNSUPPORTED, "the learned octree takes FP32 or FP16 rows");
@@ -247,6 +251,31 @@ int bpgb_octree_reconstruct(bpgb_octree oc, const float *d_H, float *d_volume, v
         if ((st = bpgb_volume_scale(d_volume, n, 1.0f, oc->absmax, kHTarget, s))) return st;
     }
     return BPGB_OK;
+}
+
+int bpgb_octree_reconstruct_host(bpgb_octree oc, const float *h_H, float *h_volume) {
+    clear_error();
+    if (!oc || !h_H || !h_volume) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    const size_t hb = (size_t)oc->P * oc->T * sizeof(float);
+    const size_t vb = (size_t)oc->fine[0] * oc->fine[1] * oc->fine[2] * sizeof(float);
+    if (!oc->io_H) {
+        cudaError_t e = cudaMalloc(&oc->io_H, hb);
+        if (e == cudaSuccess) e = cudaMalloc(&oc->io_vol, vb);
+        if (e != cudaSuccess) {
+            cudaFree(oc->io_H);
+            cudaFree(oc->io_vol);
+            oc->io_H = oc->io_vol = nullptr;
+            return e == cudaErrorMemoryAllocation ? set_error(BPGB_ERR_OUT_OF_MEMORY, "octree I/O buffers")
+                                                  : cuda_error(e, "octree I/O buffers");
+        }
+        oc->scratch += hb + vb;
+    }
+    BPGB_CUDA_TRY(cudaMemcpy(oc->io_H, h_H, hb, cudaMemcpyHostToDevice));
+    int st = bpgb_octree_reconstruct(oc, oc->io_H, oc->io_vol, nullptr);
+    if (st) return st;
+    BPGB_CUDA_TRY(cudaMemcpy(h_volume, oc->io_vol, vb, cudaMemcpyDeviceToHost));
+    uint64_t v = 0;
+    return bpgb_plan_check(oc->sparse_plan, &v);
 }
 
 int bpgb_octree_selected(bpgb_octree oc, uint32_t *tiles) {

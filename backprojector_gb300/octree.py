@@ -207,9 +207,10 @@ class OctreeGeometry:
         c = synthetic.make_capture(name, seed=0, small=small, render=False, **overrides)
         n = int(c.voxels_per_side[0])
         coarse = n // BLOCK
-        zc, ic = capi.volume_basis(c.volume_position, c.volume_size,
-                                   np.full(3, coarse, np.uint32))
-        assert np.array_equal(zc, c.zero)
+        # the coarse grid spans the same box: each step x (n - 1) / (coarse - 1), formed in
+        # FP64 from the fine steps (as bpgb_octree_create does)
+        ic = (np.asarray(c.inc, np.float64).reshape(3, 3) * (n - 1) / (coarse - 1))
+        ic = ic.astype(np.float32).reshape(-1)
         return cls(c.pairs, c.T, c.t0, c.deltaT, (n, n, n), (coarse, coarse, coarse), c.zero,
                    c.inc, ic, c.volume_position, c.volume_size, c.spec)
 

@@ -351,7 +351,7 @@ int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batc
  * trilinear fill of the whole volume; a full-resolution pass over the 8^3 blocks scoring
  * p >= p_lo (tile list, pair splits); the FP16 scale undone.  voxels_per_side must be
  * multiples of 8 (>= 16); d_H holds FP32 rows of pitch T.  opt: h_dtype F32 or F16
- * (default F16), tile (-1: 8^3 tiles), pair_splits (0: 4), chunk, stages.  p_lo <= 0
+ * (opt = NULL: FP16 rows), tile (-1: 8^3 tiles), pair_splits (0: 4), chunk, stages.  p_lo <= 0
  * takes the weights file's.  Buffers are allocated at create; reconstruct allocates
  * nothing and reads no device value on the host. */
 typedef struct bpgb_octree_info {
@@ -371,6 +371,9 @@ int bpgb_octree_create(bpgb_octree *octree, const bpgb_pair *host_pairs, uint64_
                        const float *voxel_inc, float t0, float deltaT, const char *weights_path,
                        float p_lo, const bpgb_options *opt);
 int bpgb_octree_reconstruct(bpgb_octree octree, const float *d_H, float *d_volume, void *stream);
+/* Synchronous form on host buffers (H [P][T] FP32, volume [Nx, Ny, Nz]); the first call
+ * allocates the device copies, later calls reuse them. */
+int bpgb_octree_reconstruct_host(bpgb_octree octree, const float *h_H, float *h_volume);
 /* Synchronises the last reconstruct's stream; *tiles = fine tiles it computed. */
 int bpgb_octree_selected(bpgb_octree octree, uint32_t *tiles);
 int bpgb_octree_get_info(bpgb_octree octree, bpgb_octree_info *info);
@@ -443,8 +446,9 @@ int bpgb_precompute_pairs(const float *laser_position, const float *laser_grid, 
 int bpgb_volume_basis(const float *volume_position, const float *volume_size,
                       const uint32_t *voxels_per_side, const float *wall_normal,
                       float *volume_zero_pos, float *voxel_inc);
-/* First and last time index any voxel can reach, +-100 bins, as fractional indices
- * (min over corners of the laser grid, camera grid and volume; see DESIGN notes). */
+/* First and last time index any voxel can reach, +-100 bins, as fractional indices.
+ * Bounds over every laser and camera grid point and the whole volume box (the reference,
+ * backproject.hpp:617-674, takes corners only, which can miss the shortest paths). */
 int bpgb_time_limits(const float *laser_position, const float *laser_grid, uint32_t lx,
                      uint32_t ly, const float *camera_position, const float *camera_grid,
                      uint32_t cx, uint32_t cy, const float *volume_position,

@@ -215,3 +215,49 @@ def test_native_octree_weights_file_errors(tmp_path):
     with pytest.raises(capi.BackprojectorError) as e:
         capi.NativeOctree(*args, tmp_path / "shape.npz")
     assert "cannot open" not in str(e.value) and "zip" not in str(e.value)
+
+
+def _cli():
+    from backprojector_gb300 import build
+
+    return str(build.CLI_PATH)
+
+
+def write_dataset(path, c, **override):
+    """A capture in the command-line tool's .npz layout."""
+    arrays = dict(data=c.transient_array(), camera_grid_positions=c.camera_grid,
+                  laser_grid_positions=c.laser_grid, camera_position=c.camera_position,
+                  laser_position=c.laser_position, t0=np.float32(c.t0),
+                  deltat=np.float32(c.deltaT), is_confocal=np.int64(1 if c.spec.confocal else 0),
+                  hidden_volume_position=c.volume_position, hidden_volume_size=c.volume_size)
+    arrays.update(override)
+    arrays = {k: v for k, v in arrays.items() if v is not None}
+    np.savez(path, **arrays)
+
+
+def test_cli_arguments_and_dataset_checks(tmp_path):
+    """bpgb_backprojector rejects bad flags and malformed datasets before touching a GPU."""
+    def run(*args):
+        return subprocess.run([_cli(), *map(str, args)], capture_output=True, text=True)
+
+    r = run("--help")
+    assert r.returncode == 0 and "usage: bpgb_backprojector" in r.stderr
+    assert run().returncode == 2
+    assert run("x.npz", "--bogus").returncode == 2
+    r = run("x.npz", "--cpu")
+    assert r.returncode == 1 and "no CPU path" in r.stderr
+    r = run(tmp_path / "missing.npz")
+    assert r.returncode == 1 and "cannot open" in r.stderr
+    c = synthetic.make_capture("dense_exhaustive_16", small=True, render=False)
+    write_dataset(tmp_path / "no_t0.npz", c, t0=None)
+    r = run(tmp_path / "no_t0.npz")
+    assert r.returncode == 1 and "missing array 't0'" in r.stderr
+    write_dataset(tmp_path / "shape.npz", c, data=np.zeros((2, 2, 2), np.float32))
+    r = run(tmp_path / "shape.npz")
+    assert r.returncode == 1 and "data must be" in r.stderr
+    write_dataset(tmp_path / "bounce.npz", c, data=np.zeros((*c.transient_array().shape[:4], 2, c.T),
+                                                              np.float32))
+    r = run(tmp_path / "bounce.npz")
+    assert r.returncode == 1 and "bounce" in r.stderr
+    r = run(tmp_path / "shape.npz", "--octree")
+    assert r.returncode == 1

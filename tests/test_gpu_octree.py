@@ -408,3 +408,35 @@ def test_trained_model_full_size_recall(cuda):
               f"{m['computed_fraction']:.4f} occupied-voxel rel-L2 vs FP64 oracle {err:.2e}")
         assert err <= 1e-3
     rec.close()
+
+
+def test_native_octree_matches_python_pipeline(cuda):
+    """bpgb_octree_* (one native object) against the Python Reconstructor on a full-size
+    held-out scene.  Both stage FP16 rows the same way, derive the 32^3 grid the same way
+    and run the same plans and CNN kernels, so the volumes are identical; backprojected
+    occupied voxels equal the dense pass."""
+    import torch
+
+    model, state = octree.OccupancyCNN.load(cuda)
+    geo = octree.OctreeGeometry.of("octree_256")
+    rec = octree.Reconstructor(geo, cuda)
+    rec.render(*octree.scene(geo, 3_000_003))
+    dense = rec.dense().clone()
+    py = rec.reconstruct(model, octree.logit(float(state["p_lo"])))
+    rec.stream.synchronize()
+    py = py.clone()
+    with capi.NativeOctree(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0,
+                           geo.deltaT, octree.WEIGHTS, h_dtype=capi.DTYPE_F16) as nat:
+        info = nat.info()
+        assert info["coarse"] == list(geo.coarse) and info["tile"] == [8, 8, 8]
+        out = torch.empty_like(dense)
+        nat.reconstruct(rec.H, out)
+        n_sel = nat.selected()
+        host = nat.reconstruct_host(rec.H.cpu().numpy())
+    assert np.array_equal(host, out.cpu().numpy())
+    assert torch.equal(out, py)
+    occ = rec.occupied_voxels(dense)
+    recall = ((out == dense) & occ).sum().item() / occ.sum().item()
+    assert recall >= 0.99
+    assert 0 < n_sel < 0.15 * info["tiles"]
+    rec.close()
