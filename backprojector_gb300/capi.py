@@ -169,6 +169,11 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_block_max": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
     "bpgb_upsample_trilinear": (C.c_int, [_P, _U32, _P, _U32, _P]),
     "bpgb_laplacian7": (C.c_int, [_P, _U32, _P, _P]),
+    "bpgb_capture_window": (C.c_int, [_F, C.c_uint32, C.c_uint32, _F, C.c_uint32, C.c_uint32, _F,
+                                      _F, C.c_float, C.c_float, C.c_int, _F, _F, C.c_int,
+                                      C.POINTER(C.c_int64), C.POINTER(C.c_uint32), _F]),
+    "bpgb_rows_crop": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int64, C.c_uint32,
+                                 _P, C.c_uint32, _P]),
     "bpgb_octree_create": (C.c_int, [C.POINTER(_P), _P, C.c_uint64, C.c_uint32, _U32, _F, _F,
                                      C.c_float, C.c_float, C.c_char_p, C.c_float,
                                      C.POINTER(Options)]),
@@ -738,3 +743,28 @@ class NativeOctree:
 
     def __exit__(self, *a):
         self.close()
+
+
+def capture_window(camera_grid, laser_grid, camera_position, laser_position, t0: float,
+                   deltaT: float, confocal: bool, volume_position, volume_size,
+                   t0_mode: int = 0) -> tuple[int, int, float]:
+    """(from, len, chunk_t0) of bpgb_capture_window."""
+    cg = f32(camera_grid)
+    lg = f32(laser_grid) if laser_grid is not None else np.zeros(3, np.float32)
+    fr, ln, ct = C.c_int64(), C.c_uint32(), C.c_float()
+    check(lib().bpgb_capture_window(fptr(cg), cg.shape[0], cg.shape[1], fptr(lg),
+                                    lg.shape[0] if lg.ndim == 3 else 1,
+                                    lg.shape[1] if lg.ndim == 3 else 1, fptr(f32(camera_position)),
+                                    fptr(f32(laser_position if laser_position is not None else
+                                             np.zeros(3))), float(t0), float(deltaT),
+                                    1 if confocal else 0, fptr(f32(volume_position)),
+                                    fptr(f32(volume_size)), int(t0_mode), C.byref(fr), C.byref(ln),
+                                    C.byref(ct)), "bpgb_capture_window")
+    return int(fr.value), int(ln.value), float(ct.value)
+
+
+def rows_crop(d_in, rows: int, T: int, in_pitch: int, from_: int, length: int, d_out,
+              out_pitch: int, stream=None) -> None:
+    check(lib().bpgb_rows_crop(_ptr(d_in), int(rows), int(T), int(in_pitch), int(from_),
+                               int(length), _ptr(d_out), int(out_pitch), _stream_ptr(stream)),
+          "bpgb_rows_crop")

@@ -105,6 +105,37 @@ int prepare(const float *camera_grid, uint32_t cx, uint32_t cy, const float *las
 
 extern "C" {
 
+int bpgb_capture_window(const float *camera_grid, uint32_t cx, uint32_t cy,
+                        const float *laser_grid, uint32_t lx, uint32_t ly,
+                        const float *camera_position, const float *laser_position, float t0,
+                        float deltaT, int confocal, const float *volume_position,
+                        const float *volume_size, int t0_mode, int64_t *from, uint32_t *len,
+                        float *chunk_t0) {
+    clear_error();
+    if (!camera_grid || !camera_position || !volume_position || !volume_size || !from || !len ||
+        !chunk_t0 || (!confocal && (!laser_grid || !laser_position)))
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "null capture argument");
+    if (t0_mode < 0 || t0_mode > 2) return set_error(BPGB_ERR_INVALID_ARGUMENT, "t0_mode 0, 1 or 2");
+    const float zeros3[3] = {0, 0, 0};
+    Window w;
+    int st = capture_window(laser_grid, lx, ly, camera_grid, cx, cy, camera_position,
+                            laser_position ? laser_position : zeros3, t0, deltaT, confocal,
+                            volume_position, volume_size, &w);
+    if (st) return st;
+    if (t0_mode == 2) {  // phasor: int limits (backproject.hpp:962)
+        const int mi = (int)w.m, Mi = (int)w.M;
+        if (Mi <= mi) return set_error(BPGB_ERR_INVALID_ARGUMENT, "degenerate capture time window");
+        *from = mi;
+        *len = (uint32_t)(Mi - mi);
+        *chunk_t0 = t0 + (float)mi * deltaT;
+        return BPGB_OK;
+    }
+    *from = w.from;
+    *len = w.len;
+    *chunk_t0 = t0_mode == 0 ? t0 + w.m * deltaT : t0 + (float)w.from * deltaT;
+    return BPGB_OK;
+}
+
 int bpgb_backproject_capture(const float *transient_data, uint32_t T,
                              const float *camera_grid, uint32_t cx, uint32_t cy,
                              const float *laser_grid, uint32_t lx, uint32_t ly,

@@ -50,6 +50,19 @@ __global__ void to_half_kernel(const float *__restrict__ in, uint64_t rows, uint
     }
 }
 
+// out[r][t] = in[r][from + t] for 0 <= from + t < T, else 0 (t < out_pitch).
+__global__ void crop_kernel(const float *__restrict__ in, uint64_t rows, uint32_t T,
+                            uint32_t in_pitch, int64_t from, uint32_t len,
+                            float *__restrict__ out, uint32_t out_pitch) {
+    const uint64_t n = rows * out_pitch;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = i / out_pitch, t = i - r * out_pitch;
+        const int64_t src = from + (int64_t)t;
+        out[i] = (t < len && src >= 0 && src < (int64_t)T) ? in[r * in_pitch + src] : 0.0f;
+    }
+}
+
 __global__ void scale_kernel(float *__restrict__ v, uint64_t n, float scale,
                              const float *__restrict__ d_absmax, float target) {
     const float f = scale_of(scale, d_absmax, target);
@@ -113,6 +126,21 @@ int bpgb_volume_scale(float *d_volume, uint64_t n, float scale, const float *d_a
     if (n == 0) return BPGB_OK;
     const unsigned grid = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
     scale_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_volume, n, scale, d_absmax, target);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+int bpgb_rows_crop(const float *d_in, uint64_t rows, uint32_t T, uint32_t in_pitch, int64_t from,
+                   uint32_t len, float *d_out, uint32_t out_pitch, void *stream) {
+    clear_error();
+    if (!d_in || !d_out || T == 0 || in_pitch < T || len == 0 || out_pitch < len)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad crop arguments");
+    const uint64_t n = rows * out_pitch;
+    if (n == 0) return BPGB_OK;
+    const unsigned grid = (unsigned)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16);
+    crop_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_in, rows, T, in_pitch, from, len, d_out,
+                                                      out_pitch);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;

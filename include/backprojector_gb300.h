@@ -455,6 +455,25 @@ int bpgb_time_limits(const float *laser_position, const float *laser_grid, uint3
                      const float *volume_size, float t0, float deltaT, float *min_index,
                      float *max_index);
 
+/* ---- time window on device-resident captures ------------------------------
+ * The window bp::backproject / bp::phasor_reconstruction crop a capture to
+ * (get_time_limits + get_transient_chunk, backproject.hpp:617-740): original bins
+ * [*from, *from + *len) (from may be negative: zero-padded) and the chunk's t0 for
+ * t0_mode 0 (dense, the reference's unfloored offset, :847), 1 (floored offset) or 2
+ * (phasor: limits truncated to int, :962).  bpgb_rows_crop copies that window of device
+ * rows [rows][in_pitch] into [rows][out_pitch] (zeros outside [0, T) and past len) on
+ * `stream`, so a device-resident capture is cropped without a host round trip; a plan
+ * with T = len, h_pitch = out_pitch and t0 = *chunk_t0 then reproduces
+ * bpgb_backproject_capture. */
+int bpgb_capture_window(const float *camera_grid, uint32_t cx, uint32_t cy,
+                        const float *laser_grid, uint32_t lx, uint32_t ly,
+                        const float *camera_position, const float *laser_position, float t0,
+                        float deltaT, int confocal, const float *volume_position,
+                        const float *volume_size, int t0_mode, int64_t *from, uint32_t *len,
+                        float *chunk_t0);
+int bpgb_rows_crop(const float *d_in, uint64_t rows, uint32_t T, uint32_t in_pitch, int64_t from,
+                   uint32_t len, float *d_out, uint32_t out_pitch, void *stream);
+
 /* ---- whole reconstructions (host buffers) --------------------------------
  * bp::backproject / bp::phasor_reconstruction on the GPU: time-window crop, FP64 pair
  * precompute, basis, then the backprojection.  transient_data is row-major

@@ -261,3 +261,21 @@ def test_cli_arguments_and_dataset_checks(tmp_path):
     assert r.returncode == 1 and "bounce" in r.stderr
     r = run(tmp_path / "shape.npz", "--octree")
     assert r.returncode == 1
+
+
+def test_capture_window_matches_time_limits():
+    c = synthetic.make_capture("dense_exhaustive_16", small=True, render=False)
+    m, M = capi.time_limits(c.laser_position, c.laser_grid, c.camera_position, c.camera_grid,
+                            c.volume_position, c.volume_size, c.t0, c.deltaT)
+    args = (c.camera_grid, c.laser_grid, c.camera_position, c.laser_position, c.t0, c.deltaT,
+            False, c.volume_position, c.volume_size)
+    fr, ln, ct = capi.capture_window(*args, t0_mode=0)
+    assert fr == int(np.floor(m)) and ln == int(np.ceil(M)) - int(np.floor(m))
+    assert ct == float(np.float32(c.t0) + np.float32(m) * np.float32(c.deltaT))
+    fr1, ln1, ct1 = capi.capture_window(*args, t0_mode=1)
+    assert (fr1, ln1) == (fr, ln)
+    assert ct1 == float(np.float32(c.t0) + np.float32(fr) * np.float32(c.deltaT))
+    fr2, ln2, _ = capi.capture_window(*args, t0_mode=2)
+    assert fr2 == int(m) and ln2 == int(M) - int(m)
+    with pytest.raises(capi.BackprojectorError):
+        capi.capture_window(*args, t0_mode=3)

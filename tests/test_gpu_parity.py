@@ -455,3 +455,37 @@ def test_reference_kernel_speed_on_256_capture(cuda):
           f"{c.updates / ref_ms * 1e3:.3e} updates/s; FAST {ms:.2f} ms = "
           f"{c.updates / ms * 1e3:.3e} updates/s; ratio {ref_ms / ms:.1f}")
     assert ms * 10 < ref_ms
+
+
+def test_device_crop_reproduces_capture_call(cuda):
+    """A device-resident capture cropped on the GPU (bpgb_capture_window + bpgb_rows_crop)
+    and backprojected by a plan equals bpgb_backproject_capture (which crops while copying
+    from the host) bit for bit."""
+    import torch
+
+    from backprojector_gb300 import load_nlosbpy
+
+    nl = load_nlosbpy()
+    c = _cap("dense_exhaustive_16", dict(laser_grid=(4, 4), spad_grid=(8, 8), voxels=16))
+    ref = nl.backproject(c.transient_array(), c.camera_grid, c.laser_grid, c.camera_position,
+                         c.laser_position, c.t0, c.deltaT, False, c.volume_position, c.volume_size,
+                         c.voxels_per_side, np.zeros(3, np.float32), assume_row_major=True)
+    fr, ln, ct = capi.capture_window(c.camera_grid, c.laser_grid, c.camera_position,
+                                     c.laser_position, c.t0, c.deltaT, False, c.volume_position,
+                                     c.volume_size, t0_mode=0)
+    pitch = (ln + 3) // 4 * 4
+    dH = torch.from_numpy(c.H).to(cuda)
+    crop = torch.full((c.P, pitch), float("nan"), device=cuda)
+    capi.rows_crop(dH, c.P, c.T, c.T, fr, ln, crop, pitch)
+    dV = torch.empty(tuple(int(v) for v in c.voxels_per_side), device=cuda)
+    pairs = capi.precompute_pairs(c.laser_position, c.laser_grid, c.camera_position,
+                                  c.camera_grid)  # the capture call's FP64 pair list
+    with capi.Plan(pairs, ln, c.voxels_per_side, c.zero, c.inc, ct, c.deltaT,
+                   h_pitch=pitch) as p:
+        p.execute(crop, dV)
+        p.check()
+    assert np.array_equal(dV.cpu().numpy(), ref)
+    host = crop.cpu().numpy()
+    lo, hi = max(fr, 0), min(c.T, fr + ln)
+    assert np.array_equal(host[:, lo - fr:hi - fr], c.H[:, lo:hi])
+    assert np.all(host[:, ln:] == 0) and np.all(host[:, :lo - fr] == 0)
