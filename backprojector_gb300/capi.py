@@ -169,6 +169,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_block_max": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
     "bpgb_upsample_trilinear": (C.c_int, [_P, _U32, _P, _U32, _P]),
     "bpgb_laplacian7": (C.c_int, [_P, _U32, _P, _P]),
+    "bpgb_complex_abs": (C.c_int, [_P, C.c_uint64, _P, _P]),
     "bpgb_capture_window": (C.c_int, [_F, C.c_uint32, C.c_uint32, _F, C.c_uint32, C.c_uint32, _F,
                                       _F, C.c_float, C.c_float, C.c_int, _F, _F, C.c_int,
                                       C.POINTER(C.c_int64), C.POINTER(C.c_uint32), _F]),
@@ -768,3 +769,8 @@ def rows_crop(d_in, rows: int, T: int, in_pitch: int, from_: int, length: int, d
     check(lib().bpgb_rows_crop(_ptr(d_in), int(rows), int(T), int(in_pitch), int(from_),
                                int(length), _ptr(d_out), int(out_pitch), _stream_ptr(stream)),
           "bpgb_rows_crop")
+
+
+def complex_abs(d_in, n: int, d_out, stream=None) -> None:
+    check(lib().bpgb_complex_abs(_ptr(d_in), int(n), _ptr(d_out), _stream_ptr(stream)),
+          "bpgb_complex_abs")

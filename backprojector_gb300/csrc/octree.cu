@@ -159,6 +159,15 @@ __global__ void laplacian7_kernel(const float *__restrict__ vol, uint32_t n0, ui
     }
 }
 
+__global__ void complex_abs_kernel(const float2 *__restrict__ in, uint64_t n,
+                                   float *__restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 z = in[i];
+        out[i] = sqrtf(z.x * z.x + z.y * z.y);
+    }
+}
+
 }  // namespace
 }  // namespace bpgb
 
@@ -236,6 +245,18 @@ int bpgb_laplacian7(const float *d_volume, const uint32_t *voxels_per_side, floa
     if (total == 0) return BPGB_OK;
     const unsigned grid = (unsigned)((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
     laplacian7_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_volume, n[0], n[1], n[2], d_out);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+int bpgb_complex_abs(const float *d_in, uint64_t n, float *d_out, void *stream) {
+    clear_error();
+    if (!d_in || !d_out || ((uintptr_t)d_in) % 8)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad complex_abs arguments");
+    if (n == 0) return BPGB_OK;
+    const unsigned grid = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
+    complex_abs_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const float2 *)d_in, n, d_out);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;

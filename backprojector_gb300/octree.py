@@ -480,3 +480,71 @@ def metrics(out, dense, computed, occ_vox, block: int = BLOCK) -> dict:
         "computed_fraction": float(computed.float().mean()),
     }
     return res
+
+
+# ---------------------------------------------------------------- phasor fields
+
+class PhasorOctree:
+    """Block-sparse phasor-field reconstruction: the reference's phasor path with octree
+    access (backproject.hpp:1012-1018, CPU only there, refining a threshold octree and
+    passing the uncropped t0 with cropped rows).  Here: the complex FAST pass on the 8x
+    coarser grid over the same box, block scores |coarse| (one coarse voxel per 8^3 fine
+    block), a full-resolution complex pass over the blocks scoring >= rho * max, zeros
+    elsewhere.  Phasor-field volumes are sharp (no low-frequency bump), so the coarse
+    magnitude marks the objects without a learned proposal.  t0 is the caller's (pass the
+    chunk t0 of cropped rows)."""
+
+    def __init__(self, pairs, T: int, voxels_per_side, zero, inc, t0: float, deltaT: float,
+                 device, rho: float = 0.1, fine_tile: int = 10, fine_splits: int = 4,
+                 h_pitch: int = 0):
+        import torch
+
+        self.torch = torch
+        self.device = device
+        self.rho = float(rho)
+        self.fine = tuple(int(v) for v in voxels_per_side)
+        assert all(v % BLOCK == 0 and v >= 2 * BLOCK for v in self.fine), self.fine
+        self.coarse = tuple(v // BLOCK for v in self.fine)
+        n = np.asarray(self.fine, np.float64)
+        ic = (np.asarray(inc, np.float64).reshape(3, 3) * ((n - 1) / (n // BLOCK - 1))[:, None])
+        ic = ic.astype(np.float32).reshape(-1)
+        common = dict(algo=capi.ALGO_FAST, h_dtype=capi.DTYPE_C64, h_pitch=h_pitch)
+        self.coarse_plan = capi.Plan(pairs, T, self.coarse, zero, ic, t0, deltaT, **common)
+        self.fine_plan = capi.Plan(pairs, T, self.fine, zero, inc, t0, deltaT, tile=fine_tile,
+                                   pair_splits=fine_splits, **common)
+        info = self.fine_plan.info()
+        self.tile = tuple(info["tile"])
+        self.n_tiles = int(np.prod([-(-f // t) for f, t in zip(self.fine, self.tile)]))
+        nc = int(np.prod(self.coarse))
+        self.coarse_vol = torch.empty(nc, dtype=torch.complex64, device=device)
+        self.mag = torch.empty(nc, dtype=torch.float32, device=device)
+        self.mx = torch.empty(1, dtype=torch.float32, device=device)
+        self.tile_list = torch.empty(self.n_tiles, dtype=torch.int32, device=device)
+        self.tile_count = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def dense(self, d_Hc, out, stream=None) -> None:
+        """The full-resolution complex pass of the same plan (the reference result)."""
+        self.fine_plan.execute(d_Hc, out, stream)
+
+    def reconstruct(self, d_Hc, out, stream=None) -> int:
+        """Complex volume of the selected blocks (zeros elsewhere) into `out`; returns the
+        number of fine tiles computed (one host read of the coarse maximum)."""
+        nc = self.mag.numel()
+        self.coarse_plan.execute(d_Hc, self.coarse_vol, stream)
+        capi.complex_abs(self.coarse_vol, nc, self.mag, stream)
+        capi.rows_absmax(self.mag, 1, nc, nc, self.mx, stream)
+        s = self.torch.cuda.current_stream() if stream is None else stream
+        s.synchronize()
+        threshold = self.rho * float(self.mx.item())
+        with self.torch.cuda.stream(s):
+            out.zero_()
+        self.fine_plan.select_tiles(self.mag, self.coarse, BLOCK, threshold, self.tile_list,
+                                    self.tile_count, stream)
+        self.fine_plan.execute_tiles(d_Hc, out, self.tile_list, self.tile_count, self.n_tiles,
+                                     stream)
+        s.synchronize()
+        return int(self.tile_count.item())
+
+    def close(self) -> None:
+        self.coarse_plan.close()
+        self.fine_plan.close()

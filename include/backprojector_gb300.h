@@ -295,6 +295,9 @@ int bpgb_block_max(const float *d_volume, const uint32_t *voxels_per_side, uint3
  * unfiltered backprojections).  d_out must not alias d_volume. */
 int bpgb_laplacian7(const float *d_volume, const uint32_t *voxels_per_side, float *d_out,
                     void *stream);
+/* d_out[i] = |d_in[i]| for n interleaved complex64 values (block scores of phasor
+ * volumes). */
+int bpgb_complex_abs(const float *d_in, uint64_t n, float *d_out, void *stream);
 /* d_fine = trilinear interpolation of d_coarse, both grids spanning one box with spacing
  * size / (n - 1) (the reference's voxel_inc, backproject.hpp:834-839). */
 int bpgb_upsample_trilinear(const float *d_coarse, const uint32_t *coarse_dims, float *d_fine,
