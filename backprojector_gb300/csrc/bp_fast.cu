@@ -53,6 +53,8 @@ namespace bpgb {
 
 namespace {
 
+constexpr int kPlanRows = 16;  // rows per unrolled consumer iteration: plans
+constexpr int kBatchRows = 4;  // and the batch kernel
 constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
 // row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
@@ -321,7 +323,7 @@ struct PipeShared {
 // it, so the stage ring and its barriers carry over.  Rows of H are read at
 // row_base + l * S + s (the capture's first row in a packed buffer).  Returns false when
 // a bounded wait gave up (the CTA must stop).
-template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int ROWS>
 __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *tmap,
                                           const float4 *__restrict__ spads,
                                           const float4 *__restrict__ lasers, void *out,
@@ -506,9 +508,11 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
 #pragma unroll
             for (int p = 0; p < NP; p++) part[p].zero();
         }
-        // Two rows per iteration give each warp 2 x NP independent voxel-pair chains
-        // (one for complex rows, whose accumulators already double the registers).
-#pragma unroll(PairT::kEsz == 8 ? 1 : 2)
+        // ROWS rows per unrolled iteration give the scheduler ROWS x NP independent
+        // voxel-pair chains to interleave (one row for complex rows, whose accumulators
+        // already double the registers).  Measured on the 256^3 capture: 2 rows 86.7 ms,
+        // 4 rows 84.5, 8 rows 80.9, 16 rows 80.4 (the batch kernel: 4 rows best).
+#pragma unroll(PairT::kEsz == 8 ? 1 : ROWS)
         for (uint32_t j = 0; j < nrows; j++) {
             const float4 r0 = table[2 * j];  // (c_o0, c_o1, ew, ew)
             const float D = row_d(v0, v1, r0.x, r0.y);
@@ -645,8 +649,8 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     }
     __syncthreads();
     uint64_t step = 0;
-    fast_unit<HT, K, KAHAN, CHECKED, PLANAR>(a, &tmap, spads, lasers, dst, diag, tile, split, 0,
-                                             step, sh);
+    fast_unit<HT, K, KAHAN, CHECKED, PLANAR, kPlanRows>(a, &tmap, spads, lasers, dst, diag, tile,
+                                                        split, 0, step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
@@ -1411,7 +1415,7 @@ __global__ void __launch_bounds__(288, 2)
         __syncthreads();
         if (*(volatile int *)&abort_flag) break;
         const float4 *tab = tables + cap_s.tab_off;
-        ok = fast_unit<HT, 8, false, CHECKED, PLANAR>(cap_s.a, &tmap, tab, tab + cap_s.a.S,
+        ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows>(cap_s.a, &tmap, tab, tab + cap_s.a.S,
                                                       out + cap_s.out_off, diag, u.tile, 0,
                                                       (uint32_t)cap_s.row_base, step, sh);
         if (!ok) *(volatile int *)&abort_flag = 1;
