@@ -53,6 +53,19 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest x over the ranks of the initialised process group (x itself without
+    one): the step time of a replica run is its slowest rank's."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region."""
 
@@ -272,10 +285,7 @@ def run_ours(args):
     launches = capi.launch_count() - launches0
     ms = e0.elapsed_time(e1) / args.steps
     plan.check()
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     updates = cap.updates
     value = updates * ws / (ms * 1e-3)
 
@@ -588,10 +598,7 @@ def run_batch(args):
     launches = max(capi.launch_count() - launches0, 0) + args.steps
     ms = e0.elapsed_time(e1) / args.steps
     batch.check()
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dev)
     updates = int(info["updates"])
     value = updates * ws / (ms * 1e-3)
 

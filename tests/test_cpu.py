@@ -279,3 +279,65 @@ def test_capture_window_matches_time_limits():
     assert fr2 == int(m) and ln2 == int(M) - int(m)
     with pytest.raises(capi.BackprojectorError):
         capi.capture_window(*args, t0_mode=3)
+
+
+def _max_worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world)
+    try:
+        q.put((rank, bench.max_over_ranks(1.5 + rank, "cpu")))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_bench_max_over_ranks_gloo():
+    """Replica runs time every rank and report the slowest (2 gloo ranks on the CPU)."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_max_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    assert got == [(0, 2.5), (1, 2.5)]
+    import bench
+
+    assert bench.max_over_ranks(3.0, "cpu") == 3.0  # no process group: the value itself
+
+
+def test_bench_reference_arm_two_ranks():
+    """--impl reference under torchrun with 2 ranks: rank 0 alone runs and prints one JSON
+    line, rank 1 exits 0 without work."""
+    import json
+    import socket
+    import sys
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    root = Path(__file__).resolve().parents[1]
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                        "--nproc-per-node", "2", "--master-addr", "127.0.0.1", "--master-port",
+                        str(port), str(root / "bench.py"), "--impl", "reference", "--gpus", "2",
+                        "--steps", "1", "--warmup", "1", "--workload", "dense_exhaustive_16",
+                        "--ref-sample", "8"], capture_output=True, text=True, timeout=600,
+                       cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
