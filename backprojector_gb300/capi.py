@@ -23,7 +23,7 @@ ERR_UNSUPPORTED = -5
 ERR_NO_DEVICE = -6
 ERR_WINDOW = -7
 
-DTYPE_F32, DTYPE_F16, DTYPE_BF16, DTYPE_C64 = 0, 1, 2, 3
+DTYPE_F32, DTYPE_F16, DTYPE_BF16, DTYPE_C64, DTYPE_C32 = 0, 1, 2, 3, 4
 ALGO_AUTO, ALGO_EXACT, ALGO_FAST = 0, 1, 2
 ACCUM_F32, ACCUM_KAHAN = 0, 1
 GEOMETRY_NAMES = {0: "generic", 1: "single_laser", 2: "exhaustive", 3: "confocal"}

@@ -301,6 +301,40 @@ struct Pair<float2> {
     }
 };
 
+// Complex rows stored as FP16 pairs (re, im) in one 32-bit word: each half is added to
+// its FP32 accumulator with the mixed-precision add.
+template <>
+struct Pair<__half2> {
+    static constexpr uint32_t kEsz = 4, kShift = 2;
+    float2 a0, a1;
+    __device__ __forceinline__ void zero() { a0 = a1 = make_float2(0.0f, 0.0f); }
+    __device__ __forceinline__ static void add_c16(float2 &acc, uint32_t w) {
+        const unsigned short re = (unsigned short)(w & 0xffffu), im = (unsigned short)(w >> 16);
+        asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc.x) : "h"(re));
+        asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc.y) : "h"(im));
+    }
+    __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
+        add_c16(a0, lds<uint32_t>(sm, p0));
+        add_c16(a1, lds<uint32_t>(sm, p1));
+    }
+    __device__ __forceinline__ void fold(Pair &comp, const Pair &part) {
+        kahan_add(a0.x, comp.a0.x, part.a0.x);
+        kahan_add(a0.y, comp.a0.y, part.a0.y);
+        kahan_add(a1.x, comp.a1.x, part.a1.x);
+        kahan_add(a1.y, comp.a1.y, part.a1.y);
+    }
+    __device__ __forceinline__ void finish(const Pair &comp) {
+        a0.x -= comp.a0.x;
+        a0.y -= comp.a0.y;
+        a1.x -= comp.a1.x;
+        a1.y -= comp.a1.y;
+    }
+    __device__ __forceinline__ void store(void *out, uint64_t i, int which, float s) const {
+        const float2 v = which ? a1 : a0;
+        ((float2 *)out)[i] = make_float2(v.x * s, v.y * s);
+    }
+};
+
 // Resident CTAs per SM each variant is compiled for: K = 8 two CTAs (18 warps, 96
 // registers; three CTAs at 72 registers measured 2% slower on the 256^3 capture),
 // K = 16 one CTA with room for its 16 chains.
@@ -790,6 +824,7 @@ uint32_t dtype_bytes(int dt) {
         case BPGB_DTYPE_F16:
         case BPGB_DTYPE_BF16: return 2;
         case BPGB_DTYPE_C64: return 8;
+        case BPGB_DTYPE_C32: return 4;
     }
     return 0;
 }
@@ -799,6 +834,7 @@ CUtensorMapDataType tma_type(int dt) {
         case BPGB_DTYPE_F16: return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
         case BPGB_DTYPE_BF16: return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
         case BPGB_DTYPE_C64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+        case BPGB_DTYPE_C32: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;  // one (re, im) FP16 pair
         default: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     }
 }
@@ -863,6 +899,7 @@ void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar
         case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar);
         case BPGB_DTYPE_BF16: return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar);
         case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar);
+        case BPGB_DTYPE_C32: return kernel_ptr8<__half2>(kahan, checked, planar);
         default: return kernel_ptr8<float>(kahan, checked, planar);
     }
 }
@@ -1123,7 +1160,7 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     // tile-list launches (tiles x tile voxels >= voxels)
     const size_t part_bytes =
         splits > 1 ? (size_t)splits * ntiles * a.tdim[0] * a.tdim[1] * a.tdim[2] *
-                         (dt == BPGB_DTYPE_C64 ? 8 : 4)
+                         (dt == BPGB_DTYPE_C64 || dt == BPGB_DTYPE_C32 ? 8 : 4)
                    : 0;
     e = cudaMalloc(&fp->d_tables, tab_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, 2 * sizeof(unsigned long long));
@@ -1155,7 +1192,7 @@ int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t s
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
     count_launches(1);
     if (a.splits > 1) {
-        const bool cplx = fp->dtype == BPGB_DTYPE_C64;
+        const bool cplx = fp->dtype == BPGB_DTYPE_C64 || fp->dtype == BPGB_DTYPE_C32;
         const uint64_t n = a.nvox * (cplx ? 2 : 1);
         const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8);
         if (cplx) {
@@ -1207,7 +1244,7 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
                                    fp->smem, stream));
     count_launches(1);
     if (a.splits > 1) {
-        const bool cplx = fp->dtype == BPGB_DTYPE_C64;
+        const bool cplx = fp->dtype == BPGB_DTYPE_C64 || fp->dtype == BPGB_DTYPE_C32;
         const uint64_t n = (uint64_t)max_tiles * a.tdim[0] * a.tdim[1] * a.tdim[2] * (cplx ? 2 : 1);
         const unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, 152ull * 8);
         float *o = (float *)d_out;

@@ -241,7 +241,7 @@ int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_
     bpgb_options o;
     bpgb_options_default(&o);
     if (opt) o = *opt;
-    if (o.h_dtype < BPGB_DTYPE_F32 || o.h_dtype > BPGB_DTYPE_C64)
+    if (o.h_dtype < BPGB_DTYPE_F32 || o.h_dtype > BPGB_DTYPE_C32)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "unknown h_dtype");
     if (o.h_pitch && o.h_pitch < T) return set_error(BPGB_ERR_INVALID_ARGUMENT, "h_pitch < T");
     int sms = 0;
@@ -275,7 +275,8 @@ int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_
         }
     }
     p->fz = factorize_pairs(host_pairs, num_pairs);
-    const bool low_precision = o.h_dtype == BPGB_DTYPE_F16 || o.h_dtype == BPGB_DTYPE_BF16;
+    const bool low_precision = o.h_dtype == BPGB_DTYPE_F16 || o.h_dtype == BPGB_DTYPE_BF16 ||
+                               o.h_dtype == BPGB_DTYPE_C32;
     int algo = o.algo;
     if (algo == BPGB_ALGO_AUTO || algo == BPGB_ALGO_FAST || low_precision ||
         o.accum == BPGB_ACCUM_KAHAN) {
@@ -312,7 +313,7 @@ int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *str
     if (plan->P && !d_H) return set_error(BPGB_ERR_INVALID_ARGUMENT, "d_H is null");
     cudaStream_t s = (cudaStream_t)stream;
     plan->last_stream = s;
-    const bool cplx = plan->opt.h_dtype == BPGB_DTYPE_C64;
+    const bool cplx = plan->opt.h_dtype == BPGB_DTYPE_C64 || plan->opt.h_dtype == BPGB_DTYPE_C32;
     if (plan->P == 0) {
         BPGB_CUDA_TRY(cudaMemsetAsync(d_volume, 0, plan->vol.count() * (cplx ? 8 : 4), s));
         return BPGB_OK;
@@ -463,8 +464,8 @@ int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, 
     if (num_pairs && !transient_chunk)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "transient_chunk is null");
     const int dt = o.h_dtype;
-    const size_t esz = dt == BPGB_DTYPE_C64 ? 8 : (dt == BPGB_DTYPE_F32 ? 4 : 2);
-    const size_t out_esz = dt == BPGB_DTYPE_C64 ? 8 : 4;
+    const size_t esz = dt == BPGB_DTYPE_C64 ? 8 : (dt == BPGB_DTYPE_F32 || dt == BPGB_DTYPE_C32 ? 4 : 2);
+    const size_t out_esz = dt == BPGB_DTYPE_C64 || dt == BPGB_DTYPE_C32 ? 8 : 4;
     // Rows are copied into a 16-byte aligned pitch so the TMA path applies to any T.
     const uint32_t align = (uint32_t)(16 / esz);
     const uint32_t pitch = (T + align - 1) / align * align;

@@ -62,7 +62,11 @@ typedef enum bpgb_dtype {
     BPGB_DTYPE_F32 = 0,
     BPGB_DTYPE_F16 = 1,
     BPGB_DTYPE_BF16 = 2,
-    BPGB_DTYPE_C64 = 3 /* interleaved (re, im) float pairs */
+    BPGB_DTYPE_C64 = 3, /* interleaved (re, im) float pairs */
+    BPGB_DTYPE_C32 = 4  /* interleaved (re, im) FP16 pairs with a per-capture scale (FAST
+                           only; the volume is complex64).  Half the bytes of complex64:
+                           twice the rows per pipeline stage for the wide windows of
+                           phasor-field captures. */
 } bpgb_dtype;
 
 typedef enum bpgb_algo {

@@ -45,6 +45,12 @@ def run_plan(cuda, H, pairs, N, zero, inc, t0, dT, **opt):
         dH = torch.from_numpy(Hn.astype(np.float32)).to(cuda).half()
     elif dtype == capi.DTYPE_BF16:
         dH = torch.from_numpy(Hn.astype(np.float32)).to(cuda).bfloat16()
+    elif dtype == capi.DTYPE_C32:
+        # interleaved FP16 (re, im) with a per-capture scale
+        flat = Hn.astype(np.complex64).view(np.float32)
+        scale = float(np.abs(flat).max()) / 16384.0 or 1.0
+        opt["h_scale"] = scale
+        dH = (torch.from_numpy(flat / np.float32(scale)).to(cuda)).half()
     elif cplx:
         dH = torch.from_numpy(Hn.astype(np.complex64)).to(cuda)
     else:
@@ -221,6 +227,30 @@ def test_fast_complex_vs_oracle(cuda):
                                algo=capi.ALGO_FAST, checked=1)
     assert info["algo"] == "fast" and viol == 0
     assert oracle.rel_l2(out, ref) < 5e-3
+
+
+@pytest.mark.parametrize("accum", ["plain", "kahan"])
+def test_fast_complex_fp16_rows_vs_oracle(cuda, accum):
+    """Complex rows stored as FP16 (re, im) pairs with a per-capture scale: same bins and
+    FP32 sums as complex64 rows; only the rows' rounding differs."""
+    c = _cap("phasor_128", {})
+    Hc = oracle.phasor_pulse(c.H, c.wavelength, c.deltaT)
+    ref = oracle.bp_gpu_c64(Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    acc = capi.ACCUM_KAHAN if accum == "kahan" else capi.ACCUM_F32
+    for checked in (1, 0):
+        out, info, viol = run_plan(cuda, Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                                   c.deltaT, algo=capi.ALGO_FAST, h_dtype=capi.DTYPE_C32,
+                                   accum=acc, checked=checked)
+        assert info["algo"] == "fast" and viol == 0
+        assert out.dtype == np.complex64
+        assert oracle.rel_l2(out, ref) < 5e-3
+
+
+def test_fp16_complex_rows_refused_by_exact(cuda):
+    c = _cap("phasor_128", {})
+    with pytest.raises(capi.BackprojectorError):
+        capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                  algo=capi.ALGO_EXACT, h_dtype=capi.DTYPE_C32)
 
 
 def test_fast_non_planar_wall_vs_oracle(cuda):
