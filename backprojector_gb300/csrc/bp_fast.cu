@@ -55,6 +55,8 @@ namespace {
 
 constexpr int kPlanRows = 16;  // rows per unrolled consumer iteration: plans
 constexpr int kBatchRows = 4;  // and the batch kernel
+constexpr int kC32Rows = 4;    // complex rows (FP16 pairs / complex64), whose accumulators
+constexpr int kC64Rows = 1;    // already double the registers
 constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
 // row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
@@ -222,6 +224,7 @@ struct Pair;
 template <>
 struct Pair<float> {
     static constexpr uint32_t kEsz = 4, kShift = 2;
+    static constexpr bool kCplx = false;
     float2 a;
     __device__ __forceinline__ void zero() { a = make_float2(0.0f, 0.0f); }
     __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
@@ -244,6 +247,7 @@ struct Pair<float> {
 template <int IS_BF16>
 struct PairHalf {
     static constexpr uint32_t kEsz = 2, kShift = 1;
+    static constexpr bool kCplx = false;
     float2 a;
     __device__ __forceinline__ void zero() { a = make_float2(0.0f, 0.0f); }
     __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
@@ -276,6 +280,7 @@ struct Pair<__nv_bfloat16> : PairHalf<1> {};
 template <>
 struct Pair<float2> {
     static constexpr uint32_t kEsz = 8, kShift = 3;
+    static constexpr bool kCplx = true;
     float2 a0, a1;
     __device__ __forceinline__ void zero() { a0 = a1 = make_float2(0.0f, 0.0f); }
     __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
@@ -306,12 +311,16 @@ struct Pair<float2> {
 template <>
 struct Pair<__half2> {
     static constexpr uint32_t kEsz = 4, kShift = 2;
+    static constexpr bool kCplx = true;
     float2 a0, a1;
     __device__ __forceinline__ void zero() { a0 = a1 = make_float2(0.0f, 0.0f); }
     __device__ __forceinline__ static void add_c16(float2 &acc, uint32_t w) {
-        const unsigned short re = (unsigned short)(w & 0xffffu), im = (unsigned short)(w >> 16);
-        asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc.x) : "h"(re));
-        asm("add.rn.f32.f16 %0, %1, %0;" : "+f"(acc.y) : "h"(im));
+        asm("{\n\t.reg .f16 re, im;\n\t"
+            "mov.b32 {re, im}, %2;\n\t"
+            "add.rn.f32.f16 %0, re, %0;\n\t"
+            "add.rn.f32.f16 %1, im, %1;\n\t}"
+            : "+f"(acc.x), "+f"(acc.y)
+            : "r"(w));
     }
     __device__ __forceinline__ void gather2(const unsigned char *sm, uint32_t p0, uint32_t p1) {
         add_c16(a0, lds<uint32_t>(sm, p0));
@@ -379,20 +388,26 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
     const uint64_t i0 = items * split / a.splits, i1 = items * (split + 1) / a.splits;
     const uint64_t step0 = step;
     step += i1 - i0;
+    const uint32_t count = (uint32_t)(i1 - i0);  // items < 2^32 (checked at plan build)
 
     TileGeo g;
     tile_of_block(a, tile, g);
 
     if (warp == 0) {
         // ---------------- producer ----------------
-        for (uint64_t it = i0; it < i1; it++) {
-            const uint64_t i = step0 + (it - i0);
-            const uint32_t stage = (uint32_t)(i % a.stages);
-            const uint32_t round = (uint32_t)(i / a.stages);
+        // stage / round of the ring and (laser, chunk) of the item advance by counting: no
+        // 64-bit division per stage
+        uint32_t stage = (uint32_t)(step0 % a.stages);
+        uint64_t round = step0 / a.stages;
+        uint32_t l = (uint32_t)(i0 / a.nchunks);
+        uint32_t c = (uint32_t)(i0 % a.nchunks);
+        for (uint32_t n = 0; n < count; n++) {
+            const uint64_t i = step0 + n;
             if (round > 0) {
                 // Every lane observes the consumers' release before its TMA overwrites
                 // the stage.
-                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (round - 1) & 1, a.spin_limit);
+                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (uint32_t)(round - 1) & 1,
+                                    a.spin_limit);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
@@ -407,8 +422,7 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
                 step = i;
                 return false;
             }
-            const uint64_t l = it / a.nchunks;
-            const uint64_t s0 = (it % a.nchunks) * a.chunk;
+            const uint64_t s0 = (uint64_t)c * a.chunk;
             const uint32_t nrows =
                 (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
             unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
@@ -447,6 +461,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(fb);
+            if (++stage == a.stages) stage = 0, round++;
+            if (++c == a.nchunks) c = 0, l++;
         }
         return true;
     }
@@ -492,16 +508,16 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         acc[i].zero();
         comp[i].zero();
     }
-    uint64_t cur_l = ~0ull;
+    uint32_t cur_l = ~0u;
     uint32_t violations = 0;
     const float2 magic2 = make_float2(kMagic, kMagic);
     const uint32_t row_elems = a.row_bytes / esz;
 
-    for (uint64_t it = i0; it < i1; it++) {
-        const uint64_t i = step0 + (it - i0);
-        const uint32_t stage = (uint32_t)(i % a.stages);
-        const uint32_t round = (uint32_t)(i / a.stages);
-        const uint64_t l = it / a.nchunks;
+    uint32_t stage = (uint32_t)(step0 % a.stages);
+    uint32_t phase = (uint32_t)(step0 / a.stages) & 1;
+    uint32_t l = (uint32_t)(i0 / a.nchunks);
+    uint32_t c = (uint32_t)(i0 % a.nchunks);
+    for (uint32_t n = 0; n < count; n++) {
         if (l != cur_l) {
             const float4 Lt = lasers[l];
 #pragma unroll
@@ -521,7 +537,7 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             cur_l = l;
         }
         // Every lane acquires the stage (TMA bytes and the producer's row records).
-        bool ok = mbar_wait(smem_addr(&full_bar[stage]), round & 1, a.spin_limit);
+        bool ok = mbar_wait(smem_addr(&full_bar[stage]), phase, a.spin_limit);
         ok = __all_sync(0xffffffffu, ok);
         if (!ok || *(volatile int *)&abort_flag) {
             if (lane == 0 && !ok) {
@@ -530,7 +546,7 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             }
             return false;
         }
-        const uint64_t s0 = (it % a.nchunks) * a.chunk;
+        const uint64_t s0 = (uint64_t)c * a.chunk;
         const uint32_t nrows =
             (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
         const unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
@@ -546,7 +562,7 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         // voxel-pair chains to interleave (one row for complex rows, whose accumulators
         // already double the registers).  Measured on the 256^3 capture: 2 rows 86.7 ms,
         // 4 rows 84.5, 8 rows 80.9, 16 rows 80.4 (the batch kernel: 4 rows best).
-#pragma unroll(PairT::kEsz == 8 ? 1 : ROWS)
+#pragma unroll(PairT::kCplx ? (PairT::kEsz == 8 ? kC64Rows : kC32Rows) : ROWS)
         for (uint32_t j = 0; j < nrows; j++) {
             const float4 r0 = table[2 * j];  // (c_o0, c_o1, ew, ew)
             const float D = row_d(v0, v1, r0.x, r0.y);
@@ -599,6 +615,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             for (int p = 0; p < NP; p++) acc[p].fold(comp[p], part[p]);
         }
         (void)row_elems;
+        if (++stage == a.stages) stage = 0, phase ^= 1;
+        if (++c == a.nchunks) c = 0, l++;
     }
     if (CHECKED && violations) atomicAdd(&diag[1], (unsigned long long)violations);
     if (KAHAN) {
@@ -998,6 +1016,8 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     a.table_bytes = table_bytes_of(chunk);
     a.stage_bytes = stage_bytes(chunk);
     a.nchunks = (uint32_t)((S + chunk - 1) / chunk);
+    // the kernel counts (laser, chunk) items in 32 bits
+    if (a.L * a.nchunks >= (1ull << 32)) return no("more than 2^32 (laser, chunk) items");
     return BPGB_OK;
 }
 
@@ -1674,6 +1694,8 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         a.table_bytes = table_bytes_of(chunk);
         a.stage_bytes = stage_bytes(chunk);
         a.nchunks = (uint32_t)((a.S + chunk - 1) / chunk);
+        if (a.L * a.nchunks >= (1ull << 32))
+            return set_error(BPGB_ERR_UNSUPPORTED, "more than 2^32 (laser, chunk) items");
         a.planar = planar ? 1 : 0;
         const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
         for (uint64_t t = 0; t < ntiles; t++) units.push_back({c, (uint32_t)t});

@@ -4,11 +4,14 @@
     python -m backprojector_gb300.profile_cases batch64
     python -m backprojector_gb300.profile_cases octree          # 2 learned-octree recons
     python -m backprojector_gb300.profile_cases cnn_train       # 2 CNN training steps
+    python -m backprojector_gb300.profile_cases phasor128 [--dtype f32|f16] [--tile N]
+        [--chunk C --stages S --splits K]                        # complex rows, 128^3
 
 Each case renders its seeded input on the GPU, runs the workload `--reps` times (default 2:
 one to warm, one to capture) and prints the CUDA-event time of the last repetition.
 Launch order per repetition (for `ncu -s`):
   dense256: bp_fast_kernel x1;  batch64: bp_batch_kernel x1;
+  phasor128: bp_fast_kernel, reduce_splits_kernel (pair splits > 1);
   octree: bp_fast_kernel (coarse), conv_fwd_kernel x4, upsample, select_tiles,
           bp_fast_kernel (tile list), scale;
   cnn_train: conv_fwd x4, bce, conv_wgrad + reduce x4 interleaved with conv_fwd
@@ -38,10 +41,13 @@ def _timed(torch, stream, fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["dense256", "batch64", "octree", "cnn_train"])
+    ap.add_argument("case", choices=["dense256", "batch64", "octree", "cnn_train", "phasor128"])
     ap.add_argument("--dtype", choices=["f32", "f16"], default="f32")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--stages", type=int, default=0)
+    ap.add_argument("--splits", type=int, default=0)
     args = ap.parse_args(argv)
 
     import torch
@@ -71,6 +77,26 @@ def main(argv=None):
             out["tile"] = list(rec.tile)
             out["updates_sparse"] = out["selected_tiles"] * int(np.prod(rec.tile)) * len(geo.pairs)
         rec.close()
+    elif args.case == "phasor128":
+        cap = synthetic.make_capture("phasor_128", seed=0)
+        Hc = torch.empty(cap.H.shape, dtype=torch.complex64, device=dev)
+        capi.phasor_pulse_device(torch.from_numpy(cap.H).to(dev), cap.P, cap.T, cap.T,
+                                 cap.wavelength, cap.deltaT, Hc, cap.T)
+        opt = dict(algo=capi.ALGO_FAST, tile=args.tile, chunk=args.chunk, stages=args.stages,
+                   pair_splits=args.splits, h_dtype=capi.DTYPE_C64)
+        rows = Hc
+        if args.dtype == "f16":
+            flat = torch.view_as_real(Hc)
+            scale = float(flat.abs().max()) / 16384.0 or 1.0
+            rows = (flat / scale).half().contiguous()
+            opt.update(h_dtype=capi.DTYPE_C32, h_scale=scale)
+        N = tuple(int(v) for v in cap.voxels_per_side)
+        dV = torch.empty(N, dtype=torch.complex64, device=dev)
+        torch.cuda.synchronize()
+        p = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, **opt)
+        out["ms"] = _timed(torch, s, lambda: p.execute(rows, dV, s), args.reps)
+        out["plan"] = p.info()
+        p.close()
     elif args.case == "batch64":
         caps = synthetic.make_batch(64, seed=0)
         scales = synthetic.fp16_scales(caps)
