@@ -69,6 +69,60 @@ int reserve_dynamic_smem(const void *kernel, uint32_t bytes) {
     return BPGB_OK;
 }
 
+namespace {
+
+// The host drop-in call's plan of the last geometry it saw, keyed by every input the
+// plan depends on (the pairs compared byte for byte).
+struct HostPlanCache {
+    bpgb_plan plan = nullptr;
+    std::vector<bpgb_pair> pairs;
+    std::vector<unsigned char> key;
+
+    static std::vector<unsigned char> make_key(uint64_t num_pairs, uint32_t T, const uint32_t *n,
+                                               const float *zero, const float *inc, float t0,
+                                               float deltaT, const bpgb_options &o) {
+        std::vector<unsigned char> k;
+        auto put = [&](const void *p, size_t b) {
+            const unsigned char *c = (const unsigned char *)p;
+            k.insert(k.end(), c, c + b);
+        };
+        const float none[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        put(&num_pairs, sizeof num_pairs);
+        put(&T, sizeof T);
+        put(n, 3 * sizeof(uint32_t));
+        put(zero ? zero : none, 3 * sizeof(float));
+        put(inc ? inc : none, 9 * sizeof(float));
+        put(&t0, sizeof t0);
+        put(&deltaT, sizeof deltaT);
+        put(&o, sizeof o);
+        return k;
+    }
+    bpgb_plan find(const bpgb_pair *p, uint64_t np, uint32_t T, const uint32_t *n,
+                   const float *zero, const float *inc, float t0, float deltaT,
+                   const bpgb_options &o) const {
+        if (!plan || pairs.size() != np) return nullptr;
+        if (make_key(np, T, n, zero, inc, t0, deltaT, o) != key) return nullptr;
+        if (np && std::memcmp(pairs.data(), p, np * sizeof(bpgb_pair)) != 0) return nullptr;
+        return plan;
+    }
+    void keep(bpgb_plan pl, const bpgb_pair *p, uint64_t np, uint32_t T, const uint32_t *n,
+              const float *zero, const float *inc, float t0, float deltaT,
+              const bpgb_options &o) {
+        plan = pl;
+        pairs.assign(p, p + np);
+        key = make_key(np, T, n, zero, inc, t0, deltaT, o);
+    }
+    void clear() {
+        if (plan) bpgb_plan_destroy(plan);
+        plan = nullptr;
+        pairs.clear();
+        key.clear();
+    }
+    ~HostPlanCache() { clear(); }
+};
+
+}  // namespace
+
 int DeviceBuffer::reserve(size_t need) {
     if (need <= bytes) return BPGB_OK;
     if (ptr) cudaFree(ptr);
@@ -471,10 +525,20 @@ int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, 
     const uint32_t pitch = (T + align - 1) / align * align;
     o.h_pitch = pitch;
 
-    bpgb_plan plan = nullptr;
-    int st = bpgb_plan_create(&plan, scanned_pairs, num_pairs, T, voxels_per_side,
+    // Repeated calls on one scan geometry (new transient data, same pairs, grid, t0, deltaT
+    // and options) reuse the calling thread's last plan instead of rebuilding its tables.
+    thread_local HostPlanCache cache;
+    bpgb_plan plan = cache.find(scanned_pairs, num_pairs, T, voxels_per_side, volume_zero_pos,
+                                voxel_inc, t0, deltaT, o);
+    int st = BPGB_OK;
+    if (!plan) {
+        cache.clear();
+        st = bpgb_plan_create(&plan, scanned_pairs, num_pairs, T, voxels_per_side,
                               volume_zero_pos, voxel_inc, t0, deltaT, &o);
-    if (st) return st;
+        if (st) return st;
+        cache.keep(plan, scanned_pairs, num_pairs, T, voxels_per_side, volume_zero_pos, voxel_inc,
+                   t0, deltaT, o);
+    }
     const uint64_t nvox = (uint64_t)voxels_per_side[0] * voxels_per_side[1] * voxels_per_side[2];
     thread_local DeviceBuffer dH, dV;
     st = dH.reserve(std::max<size_t>(16, num_pairs * (size_t)pitch * esz));
@@ -495,9 +559,11 @@ int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, 
         cudaError_t e = cudaMemcpy(voxel_volume, dV.ptr, nvox * out_esz, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) st = cuda_error(e, "volume download");
     }
-    const std::string keep = st ? std::string(bpgb_last_error()) : std::string();
-    bpgb_plan_destroy(plan);
-    if (st) set_error(st, keep);
+    if (st) {  // a failed call does not leave its plan for the next one
+        const std::string keep(bpgb_last_error());
+        cache.clear();
+        set_error(st, keep);
+    }
     return st;
 }
 

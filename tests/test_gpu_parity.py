@@ -356,6 +356,35 @@ def test_dropin_host_call_matches_plan(cuda):
     assert oracle.rel_l2(f, ref) < 5e-3
 
 
+def test_dropin_host_call_reuses_plan_only_for_same_geometry(cuda):
+    """The host call keeps its last plan per thread: repeated calls with new transient data
+    reuse it, and any change of pairs, grid, t0, deltaT or options builds a new one."""
+    c = _cap("precision_64", {})
+    args = (c.voxels_per_side, c.zero, c.inc)
+
+    def fresh(H, pairs, t0, dT, **opt):
+        return run_plan(cuda, H, pairs, *args, t0, dT, **opt)[0]
+
+    first = capi.backproject_host(c.H, c.pairs, *args, c.t0, c.deltaT)
+    assert np.array_equal(first, fresh(c.H, c.pairs, c.t0, c.deltaT))
+    H2 = np.ascontiguousarray(c.H[::-1])  # new data, same geometry: cached plan
+    again = capi.backproject_host(H2, c.pairs, *args, c.t0, c.deltaT)
+    assert np.array_equal(again, fresh(H2, c.pairs, c.t0, c.deltaT))
+    moved = c.pairs.copy()
+    moved["camera_point"][5, 0] += 0.01
+    for pairs, t0, dT, opt in ((moved, c.t0, c.deltaT, {}),
+                               (c.pairs, c.t0 + 3 * c.deltaT, c.deltaT, {}),
+                               (c.pairs, c.t0, c.deltaT * 1.01, {}),
+                               (c.pairs, c.t0, c.deltaT, dict(accum=capi.ACCUM_KAHAN)),
+                               (c.pairs, c.t0, c.deltaT, {})):
+        got = capi.backproject_host(c.H, pairs, *args, t0, dT, **opt)
+        assert np.array_equal(got, fresh(c.H, pairs, t0, dT, **opt))
+    grid = (c.voxels_per_side[0], c.voxels_per_side[1], c.voxels_per_side[2] - 4)
+    got = capi.backproject_host(c.H, c.pairs, grid, c.zero, c.inc, c.t0, c.deltaT)
+    assert np.array_equal(got, run_plan(cuda, c.H, c.pairs, grid, c.zero, c.inc, c.t0,
+                                        c.deltaT)[0])
+
+
 def test_empty_and_out_of_range(cuda):
     c = _cap("precision_64", {})
     empty = capi.backproject_host(np.zeros((0, c.T), np.float32), c.pairs[:0], c.voxels_per_side,
