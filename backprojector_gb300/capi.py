@@ -23,6 +23,7 @@ ERR_UNSUPPORTED = -5
 ERR_NO_DEVICE = -6
 ERR_WINDOW = -7
 
+ABI_VERSION = 2  # BPGB_ABI_VERSION of the structures mirrored below
 DTYPE_F32, DTYPE_F16, DTYPE_BF16, DTYPE_C64, DTYPE_C32 = 0, 1, 2, 3, 4
 ALGO_AUTO, ALGO_EXACT, ALGO_FAST = 0, 1, 2
 ACCUM_F32, ACCUM_KAHAN = 0, 1
@@ -38,7 +39,8 @@ class Options(C.Structure):
     _fields_ = [("algo", C.c_int32), ("h_dtype", C.c_int32), ("accum", C.c_int32),
                 ("h_pitch", C.c_uint32), ("h_scale", C.c_float), ("tile", C.c_int32),
                 ("pair_splits", C.c_int32), ("checked", C.c_int32), ("spin_limit", C.c_uint32),
-                ("chunk", C.c_int32), ("stages", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("chunk", C.c_int32), ("stages", C.c_int32), ("unfactored", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class PlanInfo(C.Structure):
@@ -46,10 +48,11 @@ class PlanInfo(C.Structure):
                 ("num_spads", C.c_uint64), ("tile", C.c_uint32 * 3), ("window", C.c_uint32),
                 ("chunk", C.c_uint32), ("stages", C.c_uint32), ("pair_splits", C.c_uint32),
                 ("grid", C.c_uint32), ("threads", C.c_uint32), ("smem_bytes", C.c_uint32),
-                ("scratch_bytes", C.c_uint64), ("updates", C.c_uint64)]
+                ("scratch_bytes", C.c_uint64), ("updates", C.c_uint64),
+                ("factored", C.c_uint32), ("reserved", C.c_uint32)]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
         d["tile"] = list(self.tile)
         d["algo"] = {1: "exact", 2: "fast"}.get(self.algo, str(self.algo))
         d["geometry"] = GEOMETRY_NAMES.get(self.geometry, str(self.geometry))
@@ -213,6 +216,10 @@ def lib() -> C.CDLL:
             raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA extension first "
                                "(python -c 'import __graft_entry__ as g; g.build()')")
         L = C.CDLL(str(LIB_PATH))
+        L.bpgb_abi_version.restype = C.c_int
+        if L.bpgb_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{LIB_PATH} has ABI {L.bpgb_abi_version()}, these bindings "
+                               f"{ABI_VERSION}: rebuild the extension")
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res

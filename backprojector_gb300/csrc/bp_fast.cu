@@ -58,6 +58,7 @@ constexpr int kBatchRows = 4;  // and the batch kernel
 constexpr int kC32Rows = 4;    // complex rows (FP16 pairs / complex64), whose accumulators
 constexpr int kC64Rows = 1;    // already double the registers
 constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
+constexpr uint32_t kFactS = 4;  // SPADs per block of the factored lasers x SPADs form
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
 // row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
 __host__ __device__ constexpr uint32_t table_bytes_of(uint32_t c) {
@@ -102,7 +103,14 @@ struct FastArgs {
     // tile-list launches with pair splits: partial sums are stored per list slot and
     // split at tile-local voxel offsets (slot-major, then split, then voxel)
     uint32_t tile_local;
+    // lasers x SPADs with factored legs (bp_fact_kernel); nchunks then counts laser groups
+    uint32_t fact;
 };
+
+// (laser, SPAD chunk) items of one tile, or (SPAD block, laser group) items when factored
+__host__ __device__ inline uint64_t fast_items(const FastArgs &a) {
+    return a.fact ? (a.S / kFactS) * (uint64_t)a.nchunks : a.L * (uint64_t)a.nchunks;
+}
 
 struct TileGeo {
     uint32_t org[3];
@@ -646,6 +654,251 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
     return true;
 }
 
+// ---- lasers x SPADs captures with factored legs ------------------------------------
+// Bin of voxel v for pair (l, s): round(A(v, l) + B(v, s)) with
+//   A = sa |v - l| + (lw - t0) / dT - lo_L(l),   B = sb |v - s| + cw / dT - lo_S(s),
+// where lo = lo_L + lo_S is the pair's staged window start (both parts aligned, so their
+// sum is).  A stage holds the rows of cl = chunk / kFactS lasers x kFactS SPADs; its table
+// carries one record per laser and per SPAD (position relative to the tile centre in bin
+// units, constant).  A consumer thread keeps B of its 8 voxels for the current SPAD block
+// in registers (formed when the block changes, reused across every laser of the capture)
+// and forms A once per laser, so an update costs two packed adds, the address and the
+// gather instead of a square root: 1 / kFactS reciprocal square roots per update.
+template <typename HT, bool CHECKED>
+__device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *tmap,
+                                          const float4 *__restrict__ spads,
+                                          const float4 *__restrict__ lasers, void *out,
+                                          unsigned long long *diag, uint32_t tile,
+                                          uint32_t split, uint64_t &step, const PipeShared &sh) {
+    using PairT = Pair<HT>;
+    constexpr uint32_t esz = PairT::kEsz;
+    constexpr int K = 8, NP = K / 2;
+    unsigned char *const smem_raw = sh.smem_raw;
+    unsigned char *const stage_base = sh.stage_base;
+    const uint32_t pad = sh.pad;
+    uint64_t *const full_bar = sh.full_bar;
+    uint64_t *const empty_bar = sh.empty_bar;
+    int &abort_flag = *sh.abort_flag;
+
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t cl = a.chunk / kFactS;  // lasers per stage
+    // items: (SPAD block, laser group), SPAD block slowest
+    const uint64_t items = fast_items(a);
+    const uint64_t i0 = items * split / a.splits, i1 = items * (split + 1) / a.splits;
+    const uint64_t step0 = step;
+    step += i1 - i0;
+    const uint32_t count = (uint32_t)(i1 - i0);
+
+    TileGeo g;
+    tile_of_block(a, tile, g);
+
+    if (warp == 0) {
+        // ---------------- producer ----------------
+        uint32_t stage = (uint32_t)(step0 % a.stages);
+        uint64_t round = step0 / a.stages;
+        uint32_t sb = (uint32_t)(i0 / a.nchunks), lg = (uint32_t)(i0 % a.nchunks);
+        const int32_t al = (int32_t)a.align;
+        for (uint32_t n = 0; n < count; n++) {
+            const uint64_t i = step0 + n;
+            if (round > 0) {
+                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (uint32_t)(round - 1) & 1,
+                                    a.spin_limit);
+                ok = __all_sync(0xffffffffu, ok);
+                if (!ok) {
+                    if (lane == 0) {
+                        atomicAdd(&diag[0], 1ull);
+                        *(volatile int *)&abort_flag = 1;
+                    }
+                    step = i;
+                    return false;
+                }
+            }
+            if (*(volatile int *)&abort_flag) {
+                step = i;
+                return false;
+            }
+            const uint32_t l0 = lg * cl;
+            const uint32_t ncl = (uint32_t)(a.L - l0 < (uint64_t)cl ? a.L - l0 : (uint64_t)cl);
+            const uint32_t s0 = sb * kFactS;
+            unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
+            float4 *table = reinterpret_cast<float4 *>(st);
+            const uint32_t data = smem_addr(st + a.table_bytes);
+            const uint32_t fb = smem_addr(&full_bar[stage]);
+            // laser records in lanes < ncl, SPAD records in lanes < kFactS
+            int32_t lo_l = 0, lo_s = 0;
+            if (lane < ncl) {
+                const float4 Lt = lasers[l0 + lane];
+                float dmin, dmax;
+                box_bounds(a, g, Lt.x, Lt.y, Lt.z, dmin, dmax);
+                lo_l = (int32_t)floorf(__fmaf_rn(a.sa, dmin, Lt.w) - kMargin);
+                lo_l -= ((lo_l % al) + al) % al;
+                const float lp[3] = {Lt.x, Lt.y, Lt.z};
+                float e[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    e[k] = __fmul_rn(lp[k] - __fmul_rn(g.ctr[k], a.h[k]), a.sa);
+                table[lane] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
+                                          sel3(e[0], e[1], e[2], a.oax1),
+                                          sel3(e[0], e[1], e[2], a.kax), Lt.w - (float)lo_l);
+            }
+            if (lane < kFactS) {
+                const float4 G = spads[s0 + lane];
+                float dmin, dmax;
+                box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
+                lo_s = (int32_t)floorf(__fmaf_rn(a.sb, dmin, G.w));
+                lo_s -= ((lo_s % al) + al) % al;
+                const float gp[3] = {G.x, G.y, G.z};
+                float e[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    e[k] = __fmul_rn(gp[k] - __fmul_rn(g.ctr[k], a.h[k]), a.sb);
+                table[cl + lane] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
+                                               sel3(e[0], e[1], e[2], a.oax1),
+                                               sel3(e[0], e[1], e[2], a.kax), G.w - (float)lo_s);
+            }
+            const uint32_t nrows = ncl * kFactS;
+            __syncwarp();
+            if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
+            __syncwarp();
+#pragma unroll
+            for (uint32_t q = 0; q < kMaxChunk / 32; q++) {
+                const uint32_t r = lane + 32 * q;  // row r = laser r / kFactS, SPAD r % kFactS
+                const int32_t x = __shfl_sync(0xffffffffu, lo_l, (r / kFactS) & 31) +
+                                  __shfl_sync(0xffffffffu, lo_s, r % kFactS);
+                if (r < nrows) {
+                    const int32_t row =
+                        (int32_t)((uint64_t)(l0 + r / kFactS) * a.S + s0 + r % kFactS);
+                    const uint32_t dst = data + r * a.row_bytes;
+                    for (uint32_t b = 0; b < a.nbox; b++)
+                        tma_load_2d(dst + b * a.BW * esz, tmap, x + (int32_t)(b * a.BW), row, fb);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(fb);
+            if (++stage == a.stages) stage = 0, round++;
+            if (++lg == a.nchunks) lg = 0, sb++;
+        }
+        return true;
+    }
+    // ---------------- consumers ----------------
+    const uint32_t cw = warp - 1;
+    const uint32_t li[3] = {lane % a.lane[0], (lane / a.lane[0]) % a.lane[1],
+                            lane / (a.lane[0] * a.lane[1])};
+    const uint32_t wi[3] = {cw % a.warp[0], (cw / a.warp[0]) % a.warp[1],
+                            cw / (a.warp[0] * a.warp[1])};
+    const uint32_t bx = g.org[0] + wi[0] * a.lane[0] * (a.kax == 0 ? K : 1) + li[0];
+    const uint32_t by = g.org[1] + wi[1] * a.lane[1] * (a.kax == 1 ? K : 1) + li[1];
+    const uint32_t bz = g.org[2] + wi[2] * a.lane[2] * (a.kax == 2 ? K : 1) + li[2];
+    const uint32_t bk = sel3(bx, by, bz, a.kax);
+    const uint32_t kstep = sel3(a.lane[0], a.lane[1], a.lane[2], a.kax);
+    const float v0 = rel_coord(a, g, a.oax0, sel3(bx, by, bz, a.oax0));
+    const float v1 = rel_coord(a, g, a.oax1, sel3(bx, by, bz, a.oax1));
+    float2 vk[NP];
+#pragma unroll
+    for (int i = 0; i < NP; i++) {
+        vk[i].x = rel_coord(a, g, a.kax, bk + (2 * i) * kstep);
+        vk[i].y = rel_coord(a, g, a.kax, bk + (2 * i + 1) * kstep);
+    }
+    // leg of the 8 voxels to the point of record rec: q * rsqrt(q) + rec.w
+    auto legs = [&](const float4 rec, float2 (&out)[NP]) {
+        const float D = row_d(v0, v1, rec.x, rec.y);
+        const float2 D2 = make_float2(D, D), nk = make_float2(-rec.z, -rec.z);
+        const float2 c2 = make_float2(rec.w, rec.w);
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            const float2 dz = __fadd2_rn(vk[p], nk);
+            const float2 q = __ffma2_rn(dz, dz, D2);
+            const float2 r = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+            out[p] = __ffma2_rn(q, r, c2);
+        }
+    };
+
+    PairT acc[NP];
+#pragma unroll
+    for (int i = 0; i < NP; i++) acc[i].zero();
+    float2 B[kFactS][NP];
+    uint32_t cur_sb = ~0u;
+    uint32_t violations = 0;
+    const float2 magic2 = make_float2(kMagic, kMagic);
+
+    uint32_t stage = (uint32_t)(step0 % a.stages);
+    uint32_t phase = (uint32_t)(step0 / a.stages) & 1;
+    uint32_t sb = (uint32_t)(i0 / a.nchunks), lg = (uint32_t)(i0 % a.nchunks);
+    for (uint32_t n = 0; n < count; n++) {
+        bool ok = mbar_wait(smem_addr(&full_bar[stage]), phase, a.spin_limit);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok || *(volatile int *)&abort_flag) {
+            if (lane == 0 && !ok) {
+                atomicAdd(&diag[0], 1ull);
+                *(volatile int *)&abort_flag = 1;
+            }
+            return false;
+        }
+        const uint32_t l0 = lg * cl;
+        const uint32_t ncl = (uint32_t)(a.L - l0 < (uint64_t)cl ? a.L - l0 : (uint64_t)cl);
+        const float4 *table =
+            reinterpret_cast<const float4 *>(stage_base + (size_t)stage * a.stage_bytes);
+        const uint32_t data = pad + stage * a.stage_bytes + a.table_bytes;  // offset from smem_raw
+        if (sb != cur_sb) {
+#pragma unroll
+            for (uint32_t si = 0; si < kFactS; si++) legs(table[cl + si], B[si]);
+            cur_sb = sb;
+        }
+        for (uint32_t lj = 0; lj < ncl; lj++) {
+            float2 A[NP];
+            legs(table[lj], A);
+#pragma unroll
+            for (uint32_t si = 0; si < kFactS; si++) {
+                const uint32_t rbase = data + (lj * kFactS + si) * a.row_bytes - kMagicBits * esz;
+#pragma unroll
+                for (int p = 0; p < NP; p++) {
+                    const float2 z = __fadd2_rn(__fadd2_rn(A[p], B[si][p]), magic2);
+                    uint32_t b0 = __float_as_uint(z.x), b1 = __float_as_uint(z.y);
+                    if (CHECKED) {
+                        const uint32_t r0i = b0 - kMagicBits, r1i = b1 - kMagicBits;
+                        if (r0i >= a.W) {
+                            violations++;
+                            b0 = kMagicBits + ((int32_t)r0i < 0 ? 0u : a.W - 1);
+                        }
+                        if (r1i >= a.W) {
+                            violations++;
+                            b1 = kMagicBits + ((int32_t)r1i < 0 ? 0u : a.W - 1);
+                        }
+                    }
+                    acc[p].gather2(smem_raw, rbase + (b0 << PairT::kShift),
+                                   rbase + (b1 << PairT::kShift));
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&empty_bar[stage]));
+        if (++stage == a.stages) stage = 0, phase ^= 1;
+        if (++lg == a.nchunks) lg = 0, sb++;
+    }
+    if (CHECKED && violations) atomicAdd(&diag[1], (unsigned long long)violations);
+    const float scale = a.splits > 1 ? 1.0f : a.out_scale;
+    const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+    const uint64_t part_off = a.splits > 1 ? (uint64_t)split * (a.tile_local ? tvox : a.nvox) : 0;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            const uint32_t kv = bk + (2 * p + w) * kstep;
+            const uint32_t x = a.kax == 0 ? kv : bx, y = a.kax == 1 ? kv : by,
+                           z = a.kax == 2 ? kv : bz;
+            if (x < a.n[0] && y < a.n[1] && z < a.n[2]) {
+                const uint64_t idx =
+                    a.tile_local
+                        ? ((uint64_t)(x - g.org[0]) * a.tdim[1] + (y - g.org[1])) * a.tdim[2] +
+                              (z - g.org[2])
+                        : ((uint64_t)x * a.n[1] + y) * a.n[2] + z;
+                acc[p].store(out, part_off + idx, w, scale);
+            }
+        }
+    }
+    return true;
+}
+
 // Producer lane 0 before the CTA exits: every stage the CTA filled must have landed
 // (bounded waits; the last `stages` steps are the only ones that can be in flight).
 __device__ __forceinline__ void pipeline_drain(uint32_t stages, uint64_t issued,
@@ -660,6 +913,51 @@ __device__ __forceinline__ void pipeline_drain(uint32_t stages, uint64_t issued,
     }
 }
 
+// The CTA's voxel tile, pair split and output base; false when a tile-list CTA has no
+// tile (it exits before any barrier is initialised).
+template <typename PairT>
+__device__ __forceinline__ bool plan_block(const FastArgs &a, void *out, uint32_t &tile,
+                                           uint32_t &split, void *&dst) {
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    tile = (uint32_t)(blockIdx.x % ntiles);
+    split = (uint32_t)(blockIdx.x / ntiles);
+    dst = out;
+    if (a.tile_list) {
+        const uint32_t slot = blockIdx.x / a.splits;
+        if (slot >= *a.tile_count) return false;
+        tile = a.tile_list[slot];
+        split = blockIdx.x % a.splits;
+        if (tile >= ntiles) return false;
+        if (a.tile_local) {
+            constexpr uint32_t kOutEsz = PairT::kCplx ? 8 : 4;
+            const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+            dst = (unsigned char *)out + (uint64_t)slot * a.splits * tvox * kOutEsz;
+        }
+    }
+    return true;
+}
+
+// Stage ring (128-byte aligned) and its mbarriers; ends with a CTA barrier.
+__device__ __forceinline__ void pipeline_init(PipeShared &sh, unsigned char *smem_raw,
+                                              uint64_t *full_bar, uint64_t *empty_bar,
+                                              int *abort_flag, uint32_t stages) {
+    sh.smem_raw = smem_raw;
+    sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;
+    sh.stage_base = smem_raw + sh.pad;
+    sh.full_bar = full_bar;
+    sh.empty_bar = empty_bar;
+    sh.abort_flag = abort_flag;
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < stages; s++) {
+            mbar_init(smem_addr(&full_bar[s]), 1);
+            mbar_init(smem_addr(&empty_bar[s]), blockDim.x / 32 - 1);
+        }
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+}
+
 template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
 __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
     bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
@@ -669,40 +967,35 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
     __shared__ __align__(8) uint64_t full_bar[8];
     __shared__ __align__(8) uint64_t empty_bar[8];
     __shared__ int abort_flag;
-    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
-    uint32_t tile = (uint32_t)(blockIdx.x % ntiles), split = (uint32_t)(blockIdx.x / ntiles);
-    void *dst = out;
-    if (a.tile_list) {  // whole-CTA exits before any barrier is initialised
-        const uint32_t slot = blockIdx.x / a.splits;
-        if (slot >= *a.tile_count) return;
-        tile = a.tile_list[slot];
-        split = blockIdx.x % a.splits;
-        if (tile >= ntiles) return;
-        if (a.tile_local) {
-            constexpr uint32_t kOutEsz = Pair<HT>::kEsz == 8 ? 8 : 4;
-            const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
-            dst = (unsigned char *)out + (uint64_t)slot * a.splits * tvox * kOutEsz;
-        }
-    }
+    uint32_t tile, split;
+    void *dst;
+    if (!plan_block<Pair<HT>>(a, out, tile, split, dst)) return;
     PipeShared sh;
-    sh.smem_raw = smem_raw;
-    sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;  // 128-byte aligned stage ring
-    sh.stage_base = smem_raw + sh.pad;
-    sh.full_bar = full_bar;
-    sh.empty_bar = empty_bar;
-    sh.abort_flag = &abort_flag;
-    if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < a.stages; s++) {
-            mbar_init(smem_addr(&full_bar[s]), 1);
-            mbar_init(smem_addr(&empty_bar[s]), blockDim.x / 32 - 1);
-        }
-        abort_flag = 0;
-        mbar_fence_init();
-    }
-    __syncthreads();
+    pipeline_init(sh, smem_raw, full_bar, empty_bar, &abort_flag, a.stages);
     uint64_t step = 0;
     fast_unit<HT, K, KAHAN, CHECKED, PLANAR, kPlanRows>(a, &tmap, spads, lasers, dst, diag, tile,
                                                         split, 0, step, sh);
+    pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
+}
+
+// Lasers x SPADs captures with factored legs (fact_unit): same launch shape as the plan
+// kernel with K = 8.
+template <typename HT, bool CHECKED>
+__global__ void __launch_bounds__(288, 2)
+    bp_fact_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
+                   const float4 *__restrict__ lasers, void *__restrict__ out,
+                   unsigned long long *__restrict__ diag, const FastArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full_bar[8];
+    __shared__ __align__(8) uint64_t empty_bar[8];
+    __shared__ int abort_flag;
+    uint32_t tile, split;
+    void *dst;
+    if (!plan_block<Pair<HT>>(a, out, tile, split, dst)) return;
+    PipeShared sh;
+    pipeline_init(sh, smem_raw, full_bar, empty_bar, &abort_flag, a.stages);
+    uint64_t step = 0;
+    fact_unit<HT, CHECKED>(a, &tmap, spads, lasers, dst, diag, tile, split, step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
@@ -787,6 +1080,37 @@ __global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
         tile_of_block(a, tile, g);
         const uint64_t l = p / a.S, s = p % a.S;
         const float4 Lt = lasers[l];
+        if (a.fact) {  // fact_unit's arithmetic: window start and legs split per laser / SPAD
+            const float4 G = spads[s];
+            const int32_t al = (int32_t)a.align;
+            float lmin, lmax, dmin, dmax;
+            box_bounds(a, g, Lt.x, Lt.y, Lt.z, lmin, lmax);
+            box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
+            int32_t lo_l = (int32_t)floorf(__fmaf_rn(a.sa, lmin, Lt.w) - kMargin);
+            lo_l -= ((lo_l % al) + al) % al;
+            int32_t lo_s = (int32_t)floorf(__fmaf_rn(a.sb, dmin, G.w));
+            lo_s -= ((lo_s % al) + al) % al;
+            const float v[3] = {rel_coord(a, g, 0, idx[0]), rel_coord(a, g, 1, idx[1]),
+                                rel_coord(a, g, 2, idx[2])};
+            auto leg = [&](float4 P4, float sc, float c) {
+                const float pp[3] = {P4.x, P4.y, P4.z};
+                float e3[3];
+                for (int k = 0; k < 3; k++) e3[k] = __fmul_rn(pp[k] - __fmul_rn(g.ctr[k], a.h[k]), sc);
+                const float D = row_d(sel3(v[0], v[1], v[2], a.oax0), sel3(v[0], v[1], v[2], a.oax1),
+                                      sel3(e3[0], e3[1], e3[2], a.oax0),
+                                      sel3(e3[0], e3[1], e3[2], a.oax1));
+                const float dz = __fadd_rn(sel3(v[0], v[1], v[2], a.kax), -sel3(e3[0], e3[1], e3[2], a.kax));
+                const float q = __fmaf_rn(dz, dz, D);
+                return __fmaf_rn(q, rsqrt_approx(q), c);
+            };
+            const float A = leg(Lt, a.sa, Lt.w - (float)lo_l);
+            const float B = leg(G, a.sb, G.w - (float)lo_s);
+            const int32_t rel =
+                (int32_t)(__float_as_uint(__fadd_rn(__fadd_rn(A, B), kMagic)) - kMagicBits);
+            const int32_t b = lo_l + lo_s + rel;
+            bins[w] = (b >= 0 && b < (int32_t)a.T) ? b : -1;
+            continue;
+        }
         float e[3], ew;
         const int32_t lo = row_record(a, g, spads[s], Lt, e, ew);
         const float A = laser_leg(a, idx, Lt);
@@ -922,13 +1246,26 @@ void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar
     }
 }
 
+void *select_fact_kernel(int dtype, bool checked) {
+    switch (dtype) {
+        case BPGB_DTYPE_F32:
+            return checked ? (void *)bp_fact_kernel<float, true> : (void *)bp_fact_kernel<float, false>;
+        case BPGB_DTYPE_F16:
+            return checked ? (void *)bp_fact_kernel<__half, true> : (void *)bp_fact_kernel<__half, false>;
+        case BPGB_DTYPE_BF16:
+            return checked ? (void *)bp_fact_kernel<__nv_bfloat16, true>
+                           : (void *)bp_fact_kernel<__nv_bfloat16, false>;
+    }
+    return nullptr;
+}
+
 // Launch arguments of the fast kernel for a volume, pair factorisation and tile preset:
 // everything but the pair splits.  No allocation.  chunk / stages > 0 override the
 // preset; otherwise the chunk shrinks until the stages fit the shared-memory budget.
 int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const double hd[3],
               bool confocal, double dT, double t0, uint64_t L, uint64_t S, uint32_t T,
               uint32_t esz, bool kahan, uint32_t chunk_req, uint32_t stages_req,
-              std::string *why, uint32_t bw_fixed = 0) {
+              std::string *why, uint32_t bw_fixed = 0, bool fact = false) {
     auto no = [&](const std::string &m) {
         if (why) *why = m;
         return BPGB_ERR_UNSUPPORTED;
@@ -973,7 +1310,9 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     }
     const double span = (sa + sb) * std::sqrt(diag2) * (1.0 + 1e-5) + 2.0 * kMargin + 3.0;
     a.align = 16 / esz;
-    const uint32_t w_need = (uint32_t)std::ceil(span) + a.align;
+    // factored form: the window start is the sum of a laser part and a SPAD part, each
+    // aligned down, so the window carries one more alignment of slack
+    const uint32_t w_need = (uint32_t)std::ceil(span) + (fact ? 2 : 1) * a.align;
     const uint32_t bw_align = 128 / esz;
     if (bw_fixed) {  // one TMA box width shared by several captures (batches)
         a.BW = bw_fixed;
@@ -987,7 +1326,7 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     a.row_bytes = a.W * esz;
     auto stage_bytes = [&](uint32_t c) { return table_bytes_of(c) + c * a.row_bytes; };
     uint32_t chunk = (uint32_t)std::min<uint64_t>(
-        std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, kMaxChunk), S);
+        std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, kMaxChunk), fact ? L * kFactS : S);
     uint32_t stages = std::min<uint32_t>(stages_req ? stages_req : cfg.stages, 8);
     if (stages < 2) stages = 2;
     // Shared memory per CTA so that the variant's resident-CTA target fits one SM (228 KB).
@@ -1011,13 +1350,20 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     if (stages * stage_bytes(chunk) > budget)
         return no("time window of one tile does not fit in shared memory (" +
                   std::to_string(a.W) + " bins)");
+    if (fact) {  // whole SPAD blocks: chunk = lasers per stage x kFactS
+        if (chunk < kFactS || S % kFactS) return no("factored form needs 4-SPAD blocks");
+        chunk = chunk / kFactS * kFactS;
+    }
     a.chunk = chunk;
     a.stages = stages;
     a.table_bytes = table_bytes_of(chunk);
     a.stage_bytes = stage_bytes(chunk);
-    a.nchunks = (uint32_t)((S + chunk - 1) / chunk);
-    // the kernel counts (laser, chunk) items in 32 bits
-    if (a.L * a.nchunks >= (1ull << 32)) return no("more than 2^32 (laser, chunk) items");
+    a.fact = fact ? 1 : 0;
+    // items: (laser, SPAD chunk), or (SPAD block, laser group) in the factored form
+    a.nchunks = fact ? (uint32_t)((L + chunk / kFactS - 1) / (chunk / kFactS))
+                     : (uint32_t)((S + chunk - 1) / chunk);
+    // the kernel counts items in 32 bits
+    if (fast_items(a) >= (1ull << 32)) return no("more than 2^32 (laser, chunk) items");
     return BPGB_OK;
 }
 
@@ -1049,7 +1395,13 @@ struct FastPlan {
     int geom = 0;
     uint32_t k = 8;
     bool planar = false;
+    bool fact = false;
 };
+
+void *plan_kernel(const FastPlan *fp) {
+    return fp->fact ? select_fact_kernel(fp->dtype, fp->checked)
+                    : select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
+}
 
 int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
                     uint64_t P, const Factorization &fz, const Volume &vol,
@@ -1078,11 +1430,17 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     const FastConfig cfg = fast_preset(opt.tile, dt);
     const bool confocal = fz.geom == GEOM_CONFOCAL;
     const uint64_t L = confocal ? 1 : fz.L;
+    // Lasers x SPADs captures take the factored form where it is built: K = 8 voxels per
+    // thread, 8 consumer warps, real rows with FP32 sums, whole 4-SPAD blocks.
+    const bool fact = fz.geom == GEOM_EXHAUSTIVE && !opt.unfactored && cfg.k == 8 &&
+                      cfg.consumer_warps() == 8 && opt.accum != BPGB_ACCUM_KAHAN &&
+                      (dt == BPGB_DTYPE_F32 || dt == BPGB_DTYPE_F16 || dt == BPGB_DTYPE_BF16) &&
+                      fz.S % kFactS == 0;
     FastArgs a;
     std::string why;
     int st = fast_args(a, cfg, vol, hd, confocal, bp.dT, bp.t0, L, fz.S, bp.T, esz,
                        opt.accum == BPGB_ACCUM_KAHAN, opt.chunk > 0 ? (uint32_t)opt.chunk : 0,
-                       opt.stages > 0 ? (uint32_t)opt.stages : 0, &why);
+                       opt.stages > 0 ? (uint32_t)opt.stages : 0, &why, 0, fact);
     if (st) return no(why);
     a.out_scale = opt.h_scale != 0.0f ? opt.h_scale : 1.0f;
     if (opt.spin_limit) a.spin_limit = opt.spin_limit;
@@ -1113,9 +1471,10 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
             planar = std::memcmp(&gk, &first, sizeof(float)) == 0;
         }
     }
-    a.planar = planar ? 1 : 0;
-    fp->planar = planar;
-    void *kern = select_kernel(dt, fp->kahan, fp->checked, fp->k, fp->planar);
+    a.planar = planar && !fact ? 1 : 0;
+    fp->planar = a.planar != 0;
+    fp->fact = fact;
+    void *kern = plan_kernel(fp);
     if (!kern) {
         delete fp;
         return no("tile preset not built for this row type / accumulation");
@@ -1133,7 +1492,7 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     }
 
     const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
-    const uint64_t items = a.L * a.nchunks;
+    const uint64_t items = fast_items(a);
     uint64_t splits = opt.pair_splits > 0 ? (uint64_t)opt.pair_splits : 1;
     if (opt.pair_splits <= 0) {
         const uint64_t want = 2ull * sm_count * occ;  // two waves of resident CTAs
@@ -1206,7 +1565,7 @@ int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t s
     void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
-    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
+    void *kern = plan_kernel(fp);
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&fp->a};
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
@@ -1257,7 +1616,7 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
     void *target = a.splits > 1 ? (void *)fp->d_partial : d_out;
-    void *kern = select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
+    void *kern = plan_kernel(fp);
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&a};
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(max_tiles * a.splits), dim3(fp->threads), args,
@@ -1363,6 +1722,7 @@ void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info) {
     info->threads = fp->threads;
     info->smem_bytes = fp->smem;
     info->scratch_bytes = fp->scratch;
+    info->factored = fp->fact ? 1 : 0;
 }
 
 int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts) {
@@ -1433,25 +1793,11 @@ __global__ void __launch_bounds__(288, 2)
     __shared__ __align__(8) uint64_t empty_bar[8];
     __shared__ int abort_flag;
     PipeShared sh;
-    sh.smem_raw = smem_raw;
-    sh.pad = (128u - (smem_addr(smem_raw) & 127u)) & 127u;
-    sh.stage_base = smem_raw + sh.pad;
-    sh.full_bar = full_bar;
-    sh.empty_bar = empty_bar;
-    sh.abort_flag = &abort_flag;
-    if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < stages; s++) {
-            mbar_init(smem_addr(&full_bar[s]), 1);
-            mbar_init(smem_addr(&empty_bar[s]), blockDim.x / 32 - 1);
-        }
-        abort_flag = 0;
-        mbar_fence_init();
-    }
+    pipeline_init(sh, smem_raw, full_bar, empty_bar, &abort_flag, stages);
     // The unit's launch descriptor is staged in shared memory: fields are reloaded from
     // there instead of held in registers (global loads would be hoisted and spill).
     __shared__ __align__(16) BatchCap cap_s;
     __shared__ uint32_t unit_s;
-    __syncthreads();
     uint64_t step = 0;
     bool ok = true;
     for (;;) {

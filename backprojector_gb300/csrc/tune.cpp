@@ -205,6 +205,7 @@ int bpgb_plan_autotune(const bpgb_pair *host_pairs, uint64_t num_pairs, uint32_t
     k << "plan/" << device_tag() << "/dt" << base.h_dtype << "/acc" << base.accum << "/P"
       << num_pairs << "/T" << T << "/n" << voxels_per_side[0] << "x" << voxels_per_side[1] << "x"
       << voxels_per_side[2] << "/dT" << deltaT << "/pitch" << (base.h_pitch ? base.h_pitch : T);
+    if (base.unfactored) k << "/unfactored";
     const std::string key = k.str();
     TuneEntry e;
     if (lookup(key, &e)) {

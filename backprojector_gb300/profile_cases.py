@@ -6,12 +6,15 @@
     python -m backprojector_gb300.profile_cases cnn_train       # 2 CNN training steps
     python -m backprojector_gb300.profile_cases phasor128 [--dtype f32|f16] [--tile N]
         [--chunk C --stages S --splits K]                        # complex rows, 128^3
+    python -m backprojector_gb300.profile_cases exhaustive32 [--unfactored] [--tile N]
+        [--chunk C --stages S --splits K]       # 16x16 lasers x 16x16 SPADs, 32^3, FP32
 
 Each case renders its seeded input on the GPU, runs the workload `--reps` times (default 2:
 one to warm, one to capture) and prints the CUDA-event time of the last repetition.
 Launch order per repetition (for `ncu -s`):
   dense256: bp_fast_kernel x1;  batch64: bp_batch_kernel x1;
   phasor128: bp_fast_kernel, reduce_splits_kernel (pair splits > 1);
+  exhaustive32: bp_fact_kernel (bp_fast_kernel with --unfactored), reduce_splits_kernel;
   octree: bp_fast_kernel (coarse), conv_fwd_kernel x4, upsample, select_tiles,
           bp_fast_kernel (tile list), scale;
   cnn_train: conv_fwd x4, bce, conv_wgrad + reduce x4 interleaved with conv_fwd
@@ -41,13 +44,15 @@ def _timed(torch, stream, fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["dense256", "batch64", "octree", "cnn_train", "phasor128"])
+    ap.add_argument("case", choices=["dense256", "batch64", "octree", "cnn_train", "phasor128",
+                                         "exhaustive32"])
     ap.add_argument("--dtype", choices=["f32", "f16"], default="f32")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--splits", type=int, default=0)
+    ap.add_argument("--unfactored", action="store_true")
     args = ap.parse_args(argv)
 
     import torch
@@ -95,6 +100,18 @@ def main(argv=None):
         torch.cuda.synchronize()
         p = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, **opt)
         out["ms"] = _timed(torch, s, lambda: p.execute(rows, dV, s), args.reps)
+        out["plan"] = p.info()
+        p.close()
+    elif args.case == "exhaustive32":
+        cap = synthetic.make_capture("dense_exhaustive_16", seed=0)
+        N = tuple(int(v) for v in cap.voxels_per_side)
+        dH = torch.from_numpy(cap.H).to(dev)
+        dV = torch.empty(N, dtype=torch.float32, device=dev)
+        p = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT,
+                      algo=capi.ALGO_FAST, tile=args.tile, chunk=args.chunk, stages=args.stages,
+                      pair_splits=args.splits, unfactored=int(args.unfactored))
+        torch.cuda.synchronize()
+        out["ms"] = _timed(torch, s, lambda: p.execute(dH, dV, s), args.reps)
         out["plan"] = p.info()
         p.close()
     elif args.case == "batch64":

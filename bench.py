@@ -327,8 +327,10 @@ def run_ours(args):
     clocks = clk.summary()
     esz = {"f32": 4, "f16": 2}[args.dtype] * (2 if phasor else 1)
     algo_bytes = cap.P * cap.T * esz + cap.nvox * (8 if phasor else 4)
+    factored = bool(info.get("factored"))
     roofline = roofline_for(updates / (ms * 1e-3), ms, algo_bytes, phasor, clocks, dev,
-                            "bp_fast_kernel" if info["algo"] == "fast" else "bp_exact_kernel")
+                            ("bp_fact_kernel" if factored else "bp_fast_kernel")
+                            if info["algo"] == "fast" else "bp_exact_kernel", factored)
     tr = ROOT / "profiles" / f"traffic_{args.workload}.json"
     if tr.exists():
         try:
@@ -698,7 +700,7 @@ def cpu_baseline_batch(caps, per_capture: int, seed: int = 0):
     return upd / secs, secs, per_capture, cores
 
 
-def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel):
+def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored=False):
     """Roofline of the FAST kernels: per-update pipe work against the pipe rates measured
     on this GPU, at the median SM clock of the timed region."""
     import torch
@@ -719,6 +721,11 @@ def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel):
                  "lds_per_sm_clk": 32.0}
         rate_src = "nominal (probe unavailable)"
     work = {"fp32": 7.0 if phasor else 6.0, "sfu": 1.0, "smem": 2.0 if phasor else 1.0}
+    if factored:
+        # lasers x SPADs with factored legs: A + B, the rounding add and the accumulate per
+        # update, plus the laser leg of each voxel (3 lanes and one rsqrt) shared by the
+        # 4 SPADs of a block
+        work = {"fp32": 3.0 + 3.4 / 4, "sfu": 1.0 / 4, "smem": 1.0}
     per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / work["fp32"],
                "sfu": rates["rsqrt_per_sm_clk"] / work["sfu"],
                "smem": rates["lds_per_sm_clk"] / work["smem"]}
@@ -730,9 +737,9 @@ def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel):
         "frac": achieved / peak_updates,
         "peak_basis": f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock in the timed region) x "
                       f"min over pipes of rate / work per update: fp32 "
-                      f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:.0f}, sfu "
-                      f"{rates['rsqrt_per_sm_clk']:.1f} rsqrt/clk / {work['sfu']:.0f}, smem "
-                      f"{rates['lds_per_sm_clk']:.1f} loads/clk / {work['smem']:.0f}; rates "
+                      f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:g}, sfu "
+                      f"{rates['rsqrt_per_sm_clk']:.1f} rsqrt/clk / {work['sfu']:g}, smem "
+                      f"{rates['lds_per_sm_clk']:.1f} loads/clk / {work['smem']:g}; rates "
                       f"{rate_src}",
         "pipe_rates_per_sm_clk": rates,
         "traffic": None,

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define BPGB_ABI_VERSION 1
+#define BPGB_ABI_VERSION 2
 
 /* One (laser point, SPAD point) pair with its origin-to-wall legs.  Byte layout is the
  * reference's CameraLaserPair: camera point first, 32 bytes. */
@@ -92,7 +92,10 @@ typedef struct bpgb_options {
     uint32_t spin_limit; /* bounded mbarrier waits: polls before giving up (0 = default) */
     int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..64 (0 = from the preset) */
     int32_t stages;      /* FAST: pipeline depth, 2..8 (0 = from the preset) */
-    int32_t reserved[5];
+    int32_t unfactored;  /* FAST, lasers x SPADs captures: 0 = per-voxel laser and SPAD legs
+                            computed once per block and reused across the other grid
+                            (default where it applies), 1 = the SPAD leg per pair */
+    int32_t reserved[4];
 } bpgb_options;
 
 /* Read-only description of a plan, for tests, the bench and the autotuner. */
@@ -111,6 +114,8 @@ typedef struct bpgb_plan_info {
     uint32_t smem_bytes; /* dynamic shared memory per CTA */
     uint64_t scratch_bytes; /* device scratch held by the plan */
     uint64_t updates;    /* voxel x pair updates per execute */
+    uint32_t factored;   /* 1 = lasers x SPADs legs factored (FAST, exhaustive captures) */
+    uint32_t reserved;
 } bpgb_plan_info;
 
 typedef struct bpgb_plan_s *bpgb_plan;

@@ -43,7 +43,7 @@ def test_library_exports_reference_cpp_entry_points():
 
 def test_abi_version_and_status_strings():
     L = capi.lib()
-    assert L.bpgb_abi_version() == 1
+    assert L.bpgb_abi_version() == capi.ABI_VERSION == 2
     assert L.bpgb_status_string(capi.ERR_TIMEOUT) == b"device wait timed out"
     o = capi.options()
     assert o.algo == capi.ALGO_AUTO and o.h_scale == 1.0 and o.tile == -1

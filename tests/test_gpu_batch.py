@@ -70,13 +70,15 @@ def test_batch_matches_plans_and_oracle(cuda, dtype):
 
     for i, c in enumerate(caps):
         assert np.all(np.isfinite(vols[i]))
-        # the same capture alone through a plan, on the same stored rows
+        # the same capture alone through a plan, on the same stored rows (lasers x SPADs
+        # captures: the per-pair form the batch kernel runs, not the factored one)
         r = b.row_offsets[i]
         dHc = torch.from_numpy(np.ascontiguousarray(H[r:r + c.P, :c.T])).to(cuda)
         dVc = torch.empty(tuple(int(v) for v in c.voxels_per_side), dtype=torch.float32,
                           device=cuda)
         with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
-                       algo=capi.ALGO_FAST, h_dtype=h_dtype, h_scale=float(scales[i])) as p:
+                       algo=capi.ALGO_FAST, h_dtype=h_dtype, h_scale=float(scales[i]),
+                       unfactored=1) as p:
             p.execute(dHc, dVc)
             p.check()
             single = dVc.cpu().numpy()

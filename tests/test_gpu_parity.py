@@ -219,6 +219,74 @@ def test_fast_matches_its_own_bin_dump(cuda):
     assert np.allclose(out.ravel()[ids], vals, rtol=1e-5, atol=1e-3)
 
 
+def _dump(cuda, c, ids, **opt):
+    import torch
+
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST, **opt) as plan:
+        d = torch.empty((len(ids), c.P), dtype=torch.int32, device=cuda)
+        plan.dump_bins(ids, d)
+        return d.cpu().numpy(), plan.info()
+
+
+@pytest.mark.parametrize("chunk,splits", [(0, 0), (4, 1), (12, 3), (64, 7)])
+def test_factored_exhaustive_vs_oracle(cuda, chunk, splits):
+    """Lasers x SPADs captures take the factored form (legs per voxel and laser / SPAD,
+    reused across the other grid); partial laser groups (12-row stages = 3 lasers over 16)
+    and pair splits that start inside a SPAD block included."""
+    c = _cap("dense_exhaustive_16", dict(laser_grid=(4, 4), spad_grid=(8, 8), voxels=16))
+    ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+    opt = dict(chunk=chunk, pair_splits=splits)
+    out, info, viol = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                               c.deltaT, algo=capi.ALGO_FAST, checked=1, **opt)
+    assert info["factored"] == 1 and info["geometry"] == "exhaustive" and viol == 0
+    assert oracle.rel_l2(out, ref) < 5e-3
+    plain, _, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                           c.deltaT, algo=capi.ALGO_FAST, **opt)
+    assert np.array_equal(plain, out)  # the checked variant changes nothing in range
+    unf, uinfo, _ = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                             c.deltaT, algo=capi.ALGO_FAST, unfactored=1, **opt)
+    assert uinfo["factored"] == 0 and oracle.rel_l2(unf, ref) < 5e-3
+    # the volume is the sum of H at the bins the dump reports (same arithmetic), and those
+    # bins match the FP64 oracle's
+    ids = np.arange(0, c.nvox, 13)
+    b, dinfo = _dump(cuda, c, ids, **opt)
+    assert dinfo["factored"] == 1
+    rows = np.arange(c.P)[None, :]
+    vals = np.where(b >= 0, c.H[rows, np.clip(b, 0, c.T - 1)], 0.0).astype(np.float64).sum(1)
+    assert np.allclose(out.ravel()[ids], vals, rtol=1e-5, atol=1e-3)
+    b64 = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT, ids, 0)
+    assert oracle.misbinned_fraction(b, b64) < 1e-2
+
+
+def test_factored_exhaustive_full_size(cuda):
+    """The 16x16 lasers x 16x16 SPADs capture at 32^3 (65,536 pairs): FP32 and FP16 rows
+    against the volume's own bin dump and the FP64 oracle's bins on sampled voxels."""
+    c = synthetic.make_capture("dense_exhaustive_16", seed=3)
+    ids = np.random.default_rng(2).choice(c.nvox, size=48, replace=False)
+    b, info = _dump(cuda, c, ids)
+    assert info["factored"] == 1
+    b64 = oracle.bins(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT, ids, 0)
+    assert oracle.misbinned_fraction(b, b64) < 1e-2
+    rows = np.arange(c.P)[None, :]
+    vals = np.where(b >= 0, c.H[rows, np.clip(b, 0, c.T - 1)], 0.0).astype(np.float64).sum(1)
+    out, _, viol = run_plan(cuda, c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0,
+                            c.deltaT, algo=capi.ALGO_FAST, checked=1)
+    assert viol == 0
+    assert np.allclose(out.ravel()[ids], vals, rtol=1e-5, atol=1e-3)
+    scale = float(np.abs(c.H).max()) / 1024.0
+    h16 = (c.H / scale).astype(np.float16)
+    out16, info16, _ = run_plan(cuda, h16.astype(np.float32), c.pairs, c.voxels_per_side, c.zero,
+                                c.inc, c.t0, c.deltaT, algo=capi.ALGO_FAST,
+                                h_dtype=capi.DTYPE_F16, h_scale=scale)
+    assert info16["factored"] == 1
+    # FP16 rows align windows to 16 bytes = 8 bins, which moves the legs' constants: a few
+    # .5-boundary bins may differ from the FP32 dump
+    vals16 = np.where(b >= 0, h16.astype(np.float64)[rows, np.clip(b, 0, c.T - 1)], 0.0).sum(1)
+    assert oracle.rel_l2(out16.ravel()[ids], vals16 * scale) < 1e-3
+    assert oracle.rel_l2(out16, out) < 5e-3
+
+
 def test_fast_complex_vs_oracle(cuda):
     c = _cap("phasor_128", {})
     Hc = oracle.phasor_pulse(c.H, c.wavelength, c.deltaT)

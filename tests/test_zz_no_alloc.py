@@ -38,8 +38,10 @@ def plan_result(cap, dH):
     import torch
 
     dV = torch.empty(tuple(int(v) for v in cap.voxels_per_side), dtype=torch.float32, device=dH.device)
+    # the no-alloc call runs the per-pair form of the FAST kernel (lasers x SPADs captures
+    # included), so it is compared with plans that do too
     with capi.Plan(cap.pairs, cap.T, cap.voxels_per_side, cap.zero, cap.inc, cap.t0, cap.deltaT,
-                   algo=capi.ALGO_FAST) as plan:
+                   algo=capi.ALGO_FAST, unfactored=1) as plan:
         plan.execute(dH, dV)
         plan.check()
     return dV.cpu().numpy()
