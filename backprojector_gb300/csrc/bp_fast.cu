@@ -669,7 +669,8 @@ __device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *
                                           const float4 *__restrict__ spads,
                                           const float4 *__restrict__ lasers, void *out,
                                           unsigned long long *diag, uint32_t tile,
-                                          uint32_t split, uint64_t &step, const PipeShared &sh) {
+                                          uint32_t split, uint32_t row_base, uint64_t &step,
+                                          const PipeShared &sh) {
     using PairT = Pair<HT>;
     constexpr uint32_t esz = PairT::kEsz;
     constexpr int K = 8, NP = K / 2;
@@ -766,8 +767,8 @@ __device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *
                 const int32_t x = __shfl_sync(0xffffffffu, lo_l, (r / kFactS) & 31) +
                                   __shfl_sync(0xffffffffu, lo_s, r % kFactS);
                 if (r < nrows) {
-                    const int32_t row =
-                        (int32_t)((uint64_t)(l0 + r / kFactS) * a.S + s0 + r % kFactS);
+                    const int32_t row = (int32_t)(row_base + (uint64_t)(l0 + r / kFactS) * a.S +
+                                                  s0 + r % kFactS);
                     const uint32_t dst = data + r * a.row_bytes;
                     for (uint32_t b = 0; b < a.nbox; b++)
                         tma_load_2d(dst + b * a.BW * esz, tmap, x + (int32_t)(b * a.BW), row, fb);
@@ -995,7 +996,7 @@ __global__ void __launch_bounds__(288, 2)
     PipeShared sh;
     pipeline_init(sh, smem_raw, full_bar, empty_bar, &abort_flag, a.stages);
     uint64_t step = 0;
-    fact_unit<HT, CHECKED>(a, &tmap, spads, lasers, dst, diag, tile, split, step, sh);
+    fact_unit<HT, CHECKED>(a, &tmap, spads, lasers, dst, diag, tile, split, 0, step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
@@ -1781,7 +1782,11 @@ struct BatchUnit {
     uint32_t cap, tile;
 };
 
-template <typename HT, bool CHECKED, bool PLANAR>
+// FACT: the launch over the batch's lasers x SPADs captures (factored legs); otherwise the
+// launch over the rest (per-pair legs).  Each is one persistent launch over its own
+// cost-sorted unit list with its own counters; a batch with both kinds runs the two
+// launches back to back.
+template <typename HT, bool CHECKED, bool PLANAR, bool FACT>
 __global__ void __launch_bounds__(288, 2)
     bp_batch_kernel(const __grid_constant__ CUtensorMap tmap, const BatchCap *__restrict__ caps,
                     const BatchUnit *__restrict__ units, uint32_t n_units,
@@ -1818,9 +1823,13 @@ __global__ void __launch_bounds__(288, 2)
         __syncthreads();
         if (*(volatile int *)&abort_flag) break;
         const float4 *tab = tables + cap_s.tab_off;
-        ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows>(cap_s.a, &tmap, tab, tab + cap_s.a.S,
-                                                      out + cap_s.out_off, diag, u.tile, 0,
-                                                      (uint32_t)cap_s.row_base, step, sh);
+        if constexpr (FACT)
+            ok = fact_unit<HT, CHECKED>(cap_s.a, &tmap, tab, tab + cap_s.a.S, out + cap_s.out_off,
+                                        diag, u.tile, 0, (uint32_t)cap_s.row_base, step, sh);
+        else
+            ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows>(
+                cap_s.a, &tmap, tab, tab + cap_s.a.S, out + cap_s.out_off, diag, u.tile, 0,
+                (uint32_t)cap_s.row_base, step, sh);
         if (!ok) *(volatile int *)&abort_flag = 1;
     }
     pipeline_drain(stages, step, full_bar, diag, spin_limit);
@@ -1835,13 +1844,21 @@ __global__ void __launch_bounds__(288, 2)
     }
 }
 
-void *select_batch_kernel(int dtype, bool checked, bool planar) {
-    if (dtype == BPGB_DTYPE_F16) {
-        if (planar) return checked ? (void *)bp_batch_kernel<__half, true, true> : (void *)bp_batch_kernel<__half, false, true>;
-        return checked ? (void *)bp_batch_kernel<__half, true, false> : (void *)bp_batch_kernel<__half, false, false>;
-    }
-    if (planar) return checked ? (void *)bp_batch_kernel<float, true, true> : (void *)bp_batch_kernel<float, false, true>;
-    return checked ? (void *)bp_batch_kernel<float, true, false> : (void *)bp_batch_kernel<float, false, false>;
+template <typename HT>
+void *batch_kernel_ptr(bool checked, bool planar, bool fact) {
+    if (fact)  // the planar-wall form is a per-pair body detail
+        return checked ? (void *)bp_batch_kernel<HT, true, false, true>
+                       : (void *)bp_batch_kernel<HT, false, false, true>;
+    if (planar)
+        return checked ? (void *)bp_batch_kernel<HT, true, true, false>
+                       : (void *)bp_batch_kernel<HT, false, true, false>;
+    return checked ? (void *)bp_batch_kernel<HT, true, false, false>
+                   : (void *)bp_batch_kernel<HT, false, false, false>;
+}
+
+void *select_batch_kernel(int dtype, bool checked, bool planar, bool fact) {
+    return dtype == BPGB_DTYPE_F16 ? batch_kernel_ptr<__half>(checked, planar, fact)
+                                   : batch_kernel_ptr<float>(checked, planar, fact);
 }
 
 }  // namespace
@@ -1850,6 +1867,9 @@ struct BatchPlan {
     int dtype = BPGB_DTYPE_F32;
     bool checked = false, planar = false;
     uint32_t n = 0, pitch = 0, stages = 0, chunk = 0, smem = 0, grid = 0, n_units = 0;
+    // units [0, n_units - n_fact) run per-pair legs, the last n_fact factored legs (a
+    // second launch with grid_fact CTAs and the counters d_sched[2..3])
+    uint32_t n_fact = 0, grid_fact = 0;
     uint32_t spin_limit = 1u << 22;
     uint64_t total_rows = 0, total_vox = 0, updates = 0;
     std::vector<uint64_t> row_off, vox_off;
@@ -1890,12 +1910,21 @@ int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (batch)");
-    void *kern = select_batch_kernel(b->dtype, b->checked, b->planar);
-    void *args[] = {(void *)&map, (void *)&b->d_caps, (void *)&b->d_units, (void *)&b->n_units,
-                    (void *)&b->d_tables, (void *)&d_out, (void *)&b->d_diag, (void *)&b->d_sched,
-                    (void *)&b->stages, (void *)&b->spin_limit};
-    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(b->grid), dim3(288), args, b->smem, s));
-    count_launches(1);
+    for (int f = 0; f < 2; f++) {
+        const uint32_t n_pp = b->n_units - b->n_fact;
+        uint32_t nu = f ? b->n_fact : n_pp;
+        if (!nu) continue;
+        const BatchUnit *units = b->d_units + (f ? n_pp : 0);
+        unsigned int *sched = b->d_sched + (f ? 2 : 0);
+        void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
+        void *args[] = {(void *)&map,         (void *)&b->d_caps, (void *)&units,
+                        (void *)&nu,          (void *)&b->d_tables, (void *)&d_out,
+                        (void *)&b->d_diag,   (void *)&sched,     (void *)&b->stages,
+                        (void *)&b->spin_limit};
+        BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(f ? b->grid_fact : b->grid), dim3(288), args,
+                                       b->smem, s));
+        count_launches(1);
+    }
     b->last_stream = s;
     return BPGB_OK;
 }
@@ -1961,9 +1990,14 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         const bool confocal = fz.geom == GEOM_CONFOCAL;
         const uint64_t L = confocal ? 1 : fz.L;
         FastArgs &a = hc[c].a;
-        st = fast_args(a, cfg, vol, hd, confocal, g.deltaT, g.t0, L, fz.S, g.T, esz, false,
-                       o.chunk > 0 ? (uint32_t)o.chunk : 0, o.stages > 0 ? (uint32_t)o.stages : 0,
-                       &why, bw);
+        bool fact = fz.geom == GEOM_EXHAUSTIVE && !o.unfactored && fz.S % kFactS == 0;
+        for (;;) {  // the per-pair form where the factored one does not fit
+            st = fast_args(a, cfg, vol, hd, confocal, g.deltaT, g.t0, L, fz.S, g.T, esz, false,
+                           o.chunk > 0 ? (uint32_t)o.chunk : 0,
+                           o.stages > 0 ? (uint32_t)o.stages : 0, &why, bw, fact);
+            if (!st || !fact) break;
+            fact = false;
+        }
         if (st) return fail(st, why);
         a.out_scale = g.h_scale != 0.0f ? g.h_scale : 1.0f;
         a.splits = 1;
@@ -2039,9 +2073,15 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         a.stages = stages;
         a.table_bytes = table_bytes_of(chunk);
         a.stage_bytes = stage_bytes(chunk);
-        a.nchunks = (uint32_t)((a.S + chunk - 1) / chunk);
-        if (a.L * a.nchunks >= (1ull << 32))
+        // factored captures need whole 4-SPAD blocks per stage; their (wider) windows
+        // serve the per-pair form as well
+        if (chunk % kFactS) a.fact = 0;
+        a.nchunks = a.fact ? (uint32_t)((a.L + chunk / kFactS - 1) / (chunk / kFactS))
+                           : (uint32_t)((a.S + chunk - 1) / chunk);
+        if (fast_items(a) >= (1ull << 32)) {
+            batch_free(b);
             return set_error(BPGB_ERR_UNSUPPORTED, "more than 2^32 (laser, chunk) items");
+        }
         a.planar = planar ? 1 : 0;
         const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
         for (uint64_t t = 0; t < ntiles; t++) units.push_back({c, (uint32_t)t});
@@ -2053,25 +2093,35 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         const FastArgs &a = hc[u.cap].a;
         return (uint64_t)a.L * a.S * a.tdim[0] * a.tdim[1] * a.tdim[2];
     };
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t x, uint32_t y) { return unit_cost(units[x]) > unit_cost(units[y]); });
+    // per-pair units first, then the factored ones; each list longest first
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const bool fx = hc[units[x].cap].a.fact != 0, fy = hc[units[y].cap].a.fact != 0;
+        if (fx != fy) return fy;
+        return unit_cost(units[x]) > unit_cost(units[y]);
+    });
     std::vector<BatchUnit> sorted(units.size());
     for (size_t i = 0; i < order.size(); i++) sorted[i] = units[order[i]];
     b->n_units = (uint32_t)sorted.size();
-    void *kern = select_batch_kernel(b->dtype, b->checked, b->planar);
-    if (int rs = reserve_dynamic_smem(kern, b->smem)) {
-        batch_free(b);
-        return rs;
+    for (const BatchUnit &u : sorted) b->n_fact += hc[u.cap].a.fact ? 1 : 0;
+    cudaError_t e = cudaSuccess;
+    for (int f = 0; f < 2; f++) {
+        const uint32_t nu = f ? b->n_fact : b->n_units - b->n_fact;
+        if (!nu) continue;
+        void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
+        if (int rs = reserve_dynamic_smem(kern, b->smem)) {
+            batch_free(b);
+            return rs;
+        }
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 288, b->smem);
+        if (e != cudaSuccess || occ < 1) {
+            batch_free(b);
+            return e != cudaSuccess ? cuda_error(e, "batch kernel attributes")
+                                    : set_error(BPGB_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
+        }
+        (f ? b->grid_fact : b->grid) = (uint32_t)std::min<uint64_t>(nu, (uint64_t)sms * occ);
     }
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 288, b->smem);
-    if (e != cudaSuccess || occ < 1) {
-        batch_free(b);
-        return e != cudaSuccess ? cuda_error(e, "batch kernel attributes")
-                                : set_error(BPGB_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
-    }
-    b->grid = (uint32_t)std::min<uint64_t>(b->n_units, (uint64_t)sms * occ);
-    e = cudaMalloc(&b->d_caps, n * sizeof(BatchCap));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_caps, n * sizeof(BatchCap));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_units, sorted.size() * sizeof(BatchUnit));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_diag, 2 * sizeof(unsigned long long));
@@ -2081,8 +2131,8 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(b->d_diag, 0, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, 2 * sizeof(unsigned int));
-    if (e == cudaSuccess) e = cudaMemset(b->d_sched, 0, 2 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, 4 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_sched, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         batch_free(b);
@@ -2109,7 +2159,7 @@ int bpgb_batch_get_info(bpgb_batch b, bpgb_batch_info *info) {
     info->total_rows = b->total_rows;
     info->total_voxels = b->total_vox;
     info->work_units = b->n_units;
-    info->grid = b->grid;
+    info->grid = std::max(b->grid, b->grid_fact);
     info->stages = b->stages;
     info->chunk = b->chunk;
     info->smem_bytes = b->smem;

@@ -1,7 +1,7 @@
 """Fixed launch sequences for profiling single kernels (ncu -k <kernel> -s <n> -c 1).
 
     python -m backprojector_gb300.profile_cases dense256 [--dtype f32|f16] [--tile N]
-    python -m backprojector_gb300.profile_cases batch64
+    python -m backprojector_gb300.profile_cases batch64 [--unfactored]
     python -m backprojector_gb300.profile_cases octree          # 2 learned-octree recons
     python -m backprojector_gb300.profile_cases cnn_train       # 2 CNN training steps
     python -m backprojector_gb300.profile_cases phasor128 [--dtype f32|f16] [--tile N]
@@ -117,7 +117,8 @@ def main(argv=None):
     elif args.case == "batch64":
         caps = synthetic.make_batch(64, seed=0)
         scales = synthetic.fp16_scales(caps)
-        b = capi.Batch(synthetic.batch_geometry(caps, scales), h_dtype=capi.DTYPE_F16)
+        b = capi.Batch(synthetic.batch_geometry(caps, scales), h_dtype=capi.DTYPE_F16,
+                       unfactored=int(args.unfactored))
         info = b.info()
         H = synthetic.pack_batch(caps, b.row_offsets, info["pitch"], np.float16, scales)
         dH = torch.from_numpy(H).to(dev)

@@ -330,7 +330,8 @@ def run_ours(args):
     factored = bool(info.get("factored"))
     roofline = roofline_for(updates / (ms * 1e-3), ms, algo_bytes, phasor, clocks, dev,
                             ("bp_fact_kernel" if factored else "bp_fast_kernel")
-                            if info["algo"] == "fast" else "bp_exact_kernel", factored)
+                            if info["algo"] == "fast" else "bp_exact_kernel",
+                            1.0 if factored else 0.0)
     tr = ROOT / "profiles" / f"traffic_{args.workload}.json"
     if tr.exists():
         try:
@@ -658,8 +659,12 @@ def run_batch(args):
                    "copied down inside each step"}
     clocks = clk.summary()
     algo_bytes = int(sum(c.P * c.T * 2 + c.nvox * 4 for c in caps))
+    # lasers x SPADs captures (whole 4-SPAD blocks) run the factored body
+    fact_updates = sum(c.updates for c in caps
+                       if len(np.unique(c.pairs["laser_point"], axis=0)) > 1
+                       and (c.P // len(np.unique(c.pairs["laser_point"], axis=0))) % 4 == 0)
     roofline = roofline_for(updates / (ms * 1e-3), ms, algo_bytes, False, clocks, dev,
-                            "bp_batch_kernel")
+                            "bp_batch_kernel", fact_updates / updates)
     line = {
         "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -700,7 +705,9 @@ def cpu_baseline_batch(caps, per_capture: int, seed: int = 0):
     return upd / secs, secs, per_capture, cores
 
 
-def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored=False):
+def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored=0.0):
+    """factored: the fraction of the updates that run the factored lasers x SPADs body
+    (1.0 for a factored plan); the peak blends the two bodies' peaks by their updates."""
     """Roofline of the FAST kernels: per-update pipe work against the pipe rates measured
     on this GPU, at the median SM clock of the timed region."""
     import torch
@@ -721,20 +728,30 @@ def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored
                  "lds_per_sm_clk": 32.0}
         rate_src = "nominal (probe unavailable)"
     work = {"fp32": 7.0 if phasor else 6.0, "sfu": 1.0, "smem": 2.0 if phasor else 1.0}
-    if factored:
-        # lasers x SPADs with factored legs: A + B, the rounding add and the accumulate per
-        # update, plus the laser leg of each voxel (3 lanes and one rsqrt) shared by the
-        # 4 SPADs of a block
-        work = {"fp32": 3.0 + 3.4 / 4, "sfu": 1.0 / 4, "smem": 1.0}
-    per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / work["fp32"],
-               "sfu": rates["rsqrt_per_sm_clk"] / work["sfu"],
-               "smem": rates["lds_per_sm_clk"] / work["smem"]}
-    bound = min(per_clk, key=per_clk.get)
-    peak_updates = sms * per_clk[bound] * sm_mhz * 1e6
+    # lasers x SPADs with factored legs: A + B, the rounding add and the accumulate per
+    # update, plus the laser leg of each voxel (3 lanes and one rsqrt) shared by the 4 SPADs
+    # of a block
+    fwork = {"fp32": 3.0 + 3.4 / 4, "sfu": 1.0 / 4, "smem": 1.0}
+
+    def body_peak(w):
+        per_clk = {"fp32": rates["fp32_lanes_per_sm_clk"] / w["fp32"],
+                   "sfu": rates["rsqrt_per_sm_clk"] / w["sfu"],
+                   "smem": rates["lds_per_sm_clk"] / w["smem"]}
+        b = min(per_clk, key=per_clk.get)
+        return b, sms * per_clk[b] * sm_mhz * 1e6
+
+    bound, peak_updates = body_peak(work)
+    fbound, fpeak = body_peak(fwork)
+    if factored >= 1.0:
+        bound, peak_updates, work = fbound, fpeak, fwork
+    elif factored > 0.0:
+        peak_updates = 1.0 / ((1.0 - factored) / peak_updates + factored / fpeak)
+        bound = f"{bound} ({1 - factored:.0%} of updates) / {fbound} ({factored:.0%}, factored)"
     return {
         "bound": bound, "kernel": kernel,
         "achieved": achieved, "peak": peak_updates, "unit": "voxel-pair updates/s",
         "frac": achieved / peak_updates,
+        "factored_fraction": factored,
         "peak_basis": f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock in the timed region) x "
                       f"min over pipes of rate / work per update: fp32 "
                       f"{rates['fp32_lanes_per_sm_clk']:.1f} lanes/clk / {work['fp32']:g}, sfu "

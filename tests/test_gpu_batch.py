@@ -25,7 +25,11 @@ def small_batch(n=10, seed=3, exhaustive_frac=0.3):
 
 
 def tol(c):
-    return 5e-3 if c.P >= 256 else 2e-2
+    # rel-L2 against the FP64 oracle is set by a handful of .5-boundary bins on small
+    # captures: one flipped bin moves a voxel by ~1/P of its sum.  Measured on the 256-pair
+    # lasers x SPADs captures: mis-binned fraction 2-4e-5 for both the factored and the
+    # per-pair form, rel-L2 up to 1.06e-2.
+    return 5e-3 if c.P >= 1024 else 2e-2
 
 
 def upload(cuda, caps, batch, dtype, scales):
@@ -71,14 +75,13 @@ def test_batch_matches_plans_and_oracle(cuda, dtype):
     for i, c in enumerate(caps):
         assert np.all(np.isfinite(vols[i]))
         # the same capture alone through a plan, on the same stored rows (lasers x SPADs
-        # captures: the per-pair form the batch kernel runs, not the factored one)
+        # captures take the factored form in both)
         r = b.row_offsets[i]
         dHc = torch.from_numpy(np.ascontiguousarray(H[r:r + c.P, :c.T])).to(cuda)
         dVc = torch.empty(tuple(int(v) for v in c.voxels_per_side), dtype=torch.float32,
                           device=cuda)
         with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
-                       algo=capi.ALGO_FAST, h_dtype=h_dtype, h_scale=float(scales[i]),
-                       unfactored=1) as p:
+                       algo=capi.ALGO_FAST, h_dtype=h_dtype, h_scale=float(scales[i])) as p:
             p.execute(dHc, dVc)
             p.check()
             single = dVc.cpu().numpy()
@@ -86,6 +89,33 @@ def test_batch_matches_plans_and_oracle(cuda, dtype):
         Hc = dequantised(c, H, b, i, scales[i])
         ref = oracle.bp_gpu_f64(Hc, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
         assert oracle.rel_l2(vols[i], ref) < tol(c), i
+
+
+@pytest.mark.parametrize("frac", [0.0, 1.0])
+def test_batch_of_one_kind(cuda, frac):
+    """Only single-laser captures (one launch, per-pair legs) or only lasers x SPADs
+    captures (one launch, factored legs); the unfactored option runs every capture per
+    pair."""
+    import torch
+
+    caps = small_batch(n=5, seed=6, exhaustive_frac=frac)
+    geo = synthetic.batch_geometry(caps)
+    outs = []
+    for unf in (0, 1):
+        with capi.Batch(geo, h_dtype=capi.DTYPE_F32, checked=1, unfactored=unf) as b:
+            H, dH, dV = upload(cuda, caps, b, np.float32, None)
+            launches = capi.launch_count()
+            b.execute(dH, dV)
+            torch.cuda.synchronize()
+            assert capi.launch_count() - launches == 1
+            assert b.check() == 0
+            outs.append(volumes(caps, b, dV.cpu().numpy()))
+    for i, c in enumerate(caps):
+        ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+        for vols in outs:
+            assert oracle.rel_l2(vols[i], ref) < tol(c), i
+        if frac == 0.0:  # nothing to factor: both runs are the same launch
+            assert np.array_equal(outs[0][i], outs[1][i])
 
 
 def test_batch_graph_replays_and_recaptures(cuda):
