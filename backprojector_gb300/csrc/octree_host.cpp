@@ -30,7 +30,7 @@ struct Layer {
 
 struct bpgb_octree_s {
     uint32_t fine[3] = {0, 0, 0}, coarse[3] = {0, 0, 0}, tile[3] = {0, 0, 0};
-    uint32_t tiles = 0, in_channels = 2, pair_splits = 4;
+    uint32_t tiles = 0, in_channels = 2, pair_splits = 8;
     uint64_t P = 0;
     uint32_t T = 0, pitch16 = 0;
     int h_dtype = BPGB_DTYPE_F16;
@@ -112,7 +112,7 @@ int bpgb_octree_create(bpgb_octree *out, const bpgb_pair *pairs, uint64_t num_pa
     oc->P = num_pairs;
     oc->T = T;
     oc->h_dtype = o.h_dtype;
-    oc->pair_splits = o.pair_splits > 0 ? (uint32_t)o.pair_splits : 4u;
+    oc->pair_splits = o.pair_splits > 0 ? (uint32_t)o.pair_splits : 8u;
     for (int k = 0; k < 3; k++) {
         oc->fine[k] = voxels_per_side[k];
         oc->coarse[k] = voxels_per_side[k] / kBlock;

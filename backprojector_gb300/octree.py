@@ -234,7 +234,7 @@ class Reconstructor:
     back at the end of each pass)."""
 
     def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = 10,
-                 h_dtype: int = capi.DTYPE_F16, fine_splits: int = 4, **fine_opt):
+                 h_dtype: int = capi.DTYPE_F16, fine_splits: int = 8, **fine_opt):
         import torch
 
         self.torch = torch

@@ -363,7 +363,7 @@ int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batc
  * trilinear fill of the whole volume; a full-resolution pass over the 8^3 blocks scoring
  * p >= p_lo (tile list, pair splits); the FP16 scale undone.  voxels_per_side must be
  * multiples of 8 (>= 16); d_H holds FP32 rows of pitch T.  opt: h_dtype F32 or F16
- * (opt = NULL: FP16 rows), tile (-1: 8^3 tiles), pair_splits (0: 4), chunk, stages.  p_lo <= 0
+ * (opt = NULL: FP16 rows), tile (-1: 8^3 tiles), pair_splits (0: 8), chunk, stages.  p_lo <= 0
  * takes the weights file's.  Buffers are allocated at create; reconstruct allocates
  * nothing and reads no device value on the host. */
 typedef struct bpgb_octree_info {
