@@ -209,13 +209,37 @@ __device__ __forceinline__ uint32_t window_bits(float vk, float D, float A, floa
 }
 
 // ---- shared-memory gathers ------------------------------------------------------------
-// Plain loads at a byte offset from the dynamic shared-memory base: the compiler sees them
-// as shared-memory reads, keeps them between the stage's full-barrier wait and its
-// empty-barrier arrive (asm with memory clobbers) and is free to interleave the
-// independent voxel chains in between.
+// `ld.shared` at a 32-bit shared-window address (the dynamic base's window address plus a
+// byte offset): one address add per gather.  Written as volatile asm they keep their
+// order against the stage's full-barrier wait and empty-barrier arrive (volatile asm
+// too); the backend still interleaves the independent voxel chains around them.  The same
+// loads written as C++ dereferences of the generic base pointer ran 9-12% slower (dense
+// 256^3 79.3 against 71.9 ms, the 64-capture batch 115.5 against 101.3 ms).
 template <typename T>
-__device__ __forceinline__ T lds(const unsigned char *smem, uint32_t off) {
-    return *reinterpret_cast<const T *>(smem + off);
+__device__ __forceinline__ T lds(const unsigned char *smem, uint32_t off);
+template <>
+__device__ __forceinline__ float lds<float>(const unsigned char *smem, uint32_t off) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(smem_addr(smem) + off));
+    return v;
+}
+template <>
+__device__ __forceinline__ unsigned short lds<unsigned short>(const unsigned char *smem, uint32_t off) {
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(smem_addr(smem) + off));
+    return v;
+}
+template <>
+__device__ __forceinline__ uint32_t lds<uint32_t>(const unsigned char *smem, uint32_t off) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(smem_addr(smem) + off));
+    return v;
+}
+template <>
+__device__ __forceinline__ float2 lds<float2>(const unsigned char *smem, uint32_t off) {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(smem_addr(smem) + off));
+    return v;
 }
 
 __device__ __forceinline__ void kahan_add(float &sum, float &comp, float x) {
