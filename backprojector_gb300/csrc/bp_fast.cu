@@ -376,12 +376,18 @@ struct Pair<__half2> {
     }
 };
 
-// Resident CTAs per SM each variant is compiled for: K = 8 two CTAs (18 warps, 96
-// registers; three CTAs at 72 registers measured 2% slower on the 256^3 capture),
-// K = 16 one CTA with room for its 16 chains.
+// Resident CTAs per SM of the 8-consumer-warp presets: K = 8 three CTAs (27 warps, 72
+// registers, no spills for real rows; with the shared-load gathers this measured 256^3
+// 71.8 -> 70.5 ms and the phasor capture's 8-row stages 16.8 -> 13.1 ms against two CTAs
+// at 96 registers), Kahan-compensated variants two (at 72 registers they spill 36-364 B),
+// K = 16 one CTA with room for its 16 chains.  The 2- and 4-warp block-sparse presets run
+// the two-CTA build (96 registers; the learned octree's fine pass measured 3.94 against
+// 4.10 ms per reconstruction with the 72-register one), and the factored lasers x SPADs
+// body keeps two (kFactCtas: its SPAD legs alone take 32 registers).
 __host__ __device__ constexpr int fast_ctas_per_sm(int k, bool kahan, int esz) {
-    return (void)kahan, (void)esz, k == 16 ? 1 : 2;
+    return (void)esz, k == 16 ? 1 : (kahan ? 2 : 3);
 }
+constexpr int kFactCtas = 2;
 
 // Shared-memory state of a CTA's pipeline: stage ring, its mbarriers, the abort flag.
 struct PipeShared {
@@ -983,8 +989,9 @@ __device__ __forceinline__ void pipeline_init(PipeShared &sh, unsigned char *sme
     __syncthreads();
 }
 
-template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR>
-__global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz))
+// CTAS: resident CTAs per SM the variant is compiled for (its register budget).
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int CTAS>
+__global__ void __launch_bounds__(288, CTAS)
     bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
                    const float4 *__restrict__ lasers, void *__restrict__ out,
                    unsigned long long *__restrict__ diag, const FastArgs a) {
@@ -1006,7 +1013,7 @@ __global__ void __launch_bounds__(288, fast_ctas_per_sm(K, KAHAN, Pair<HT>::kEsz
 // Lasers x SPADs captures with factored legs (fact_unit): same launch shape as the plan
 // kernel with K = 8.
 template <typename HT, bool CHECKED>
-__global__ void __launch_bounds__(288, 2)
+__global__ void __launch_bounds__(288, kFactCtas)
     bp_fact_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
                    const float4 *__restrict__ lasers, void *__restrict__ out,
                    unsigned long long *__restrict__ diag, const FastArgs a) {
@@ -1240,34 +1247,40 @@ const FastConfig kPresets[] = {
     {8, 1, 4, 8, 2, 1, 2, 1, 64, 4},  // 16 x 8 x 8
 };
 
+// wide: a preset with 8 consumer warps (three CTAs per SM unless Kahan-compensated)
 template <typename HT, int K, bool PLANAR>
-void *kernel_ptr(bool kahan, bool checked) {
+void *kernel_ptr(bool kahan, bool checked, bool wide) {
     if (kahan)
-        return checked ? (void *)bp_fast_kernel<HT, K, true, true, PLANAR>
-                       : (void *)bp_fast_kernel<HT, K, true, false, PLANAR>;
-    return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR>
-                   : (void *)bp_fast_kernel<HT, K, false, false, PLANAR>;
+        return checked ? (void *)bp_fast_kernel<HT, K, true, true, PLANAR, 2>
+                       : (void *)bp_fast_kernel<HT, K, true, false, PLANAR, 2>;
+    if (wide)
+        return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 3>
+                       : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 3>;
+    return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 2>
+                   : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 2>;
 }
 
 template <typename HT>
-void *kernel_ptr8(bool kahan, bool checked, bool planar) {
-    return planar ? kernel_ptr<HT, 8, true>(kahan, checked) : kernel_ptr<HT, 8, false>(kahan, checked);
+void *kernel_ptr8(bool kahan, bool checked, bool planar, bool wide) {
+    return planar ? kernel_ptr<HT, 8, true>(kahan, checked, wide)
+                  : kernel_ptr<HT, 8, false>(kahan, checked, wide);
 }
 
-// Variants built: K = 8 for every row type, accumulation, check mode and wall shape;
-// K = 16 (one CTA per SM, 16 chains per thread) for FP32 rows with plain sums.
-void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar) {
+// Variants built: K = 8 for every row type, accumulation, check mode and wall shape, in
+// the 72-register (8-warp presets, plain sums) and 96-register builds; K = 16 (one CTA
+// per SM, 16 chains per thread) for FP32 rows with plain sums.
+void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar, bool wide) {
     if (k == 16) {
         if (dtype != BPGB_DTYPE_F32 || kahan) return nullptr;
-        return checked ? (void *)bp_fast_kernel<float, 16, false, true, false>
-                       : (void *)bp_fast_kernel<float, 16, false, false, false>;
+        return checked ? (void *)bp_fast_kernel<float, 16, false, true, false, 1>
+                       : (void *)bp_fast_kernel<float, 16, false, false, false, 1>;
     }
     switch (dtype) {
-        case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar);
-        case BPGB_DTYPE_BF16: return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar);
-        case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar);
-        case BPGB_DTYPE_C32: return kernel_ptr8<__half2>(kahan, checked, planar);
-        default: return kernel_ptr8<float>(kahan, checked, planar);
+        case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar, wide);
+        case BPGB_DTYPE_BF16: return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar, wide);
+        case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar, wide);
+        case BPGB_DTYPE_C32: return kernel_ptr8<__half2>(kahan, checked, planar, wide);
+        default: return kernel_ptr8<float>(kahan, checked, planar, wide);
     }
 }
 
@@ -1357,7 +1370,7 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     // Shared memory per CTA so that the variant's resident-CTA target fits one SM (228 KB).
     // Smaller CTAs (2 or 4 consumer warps, block-sparse tiles) need proportionally more
     // resident CTAs per SM: 96 registers x (1 + warps) x 32 threads each.
-    const int ctas = cwarps == 8 ? fast_ctas_per_sm((int)cfg.k, kahan, (int)esz)
+    const int ctas = cwarps == 8 ? (fact ? kFactCtas : fast_ctas_per_sm((int)cfg.k, kahan, (int)esz))
                                  : (cwarps == 4 ? 4 : 7);
     const uint32_t soft = ctas >= 7   ? 38 * 1024
                           : ctas >= 4 ? 56 * 1024
@@ -1421,11 +1434,13 @@ struct FastPlan {
     uint32_t k = 8;
     bool planar = false;
     bool fact = false;
+    bool wide = true;  // 8 consumer warps per CTA
 };
 
 void *plan_kernel(const FastPlan *fp) {
     return fp->fact ? select_fact_kernel(fp->dtype, fp->checked)
-                    : select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar);
+                    : select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar,
+                                    fp->wide);
 }
 
 int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
@@ -1481,6 +1496,7 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     fp->smem = fast_smem(a);
 
     fp->k = cfg.k;
+    fp->wide = cfg.consumer_warps() == 8;
     // Planar wall: every SPAD's frame coordinate along the voxel-line axis is the same
     // float (the table below computes the same value per SPAD).
     bool planar = cfg.k == 8;
@@ -2436,7 +2452,7 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     if (st) return set_error(st, why);
     const uint32_t threads = fast_threads(cfg);
     const uint32_t smem = fast_smem(a);
-    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, false);  // general form first
+    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, false, true);  // general form first
     st = reserve_dynamic_smem(kern, smem);
     if (st) return st;
     int occ = 0;
@@ -2488,7 +2504,7 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     // lies on one plane across the voxel lines.
     if (h[4] == 0 && cfg.k == 8) {
         a.planar = 1;
-        kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, true);
+        kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, true, true);
         st = reserve_dynamic_smem(kern, smem);
         if (st) return st;
     }
