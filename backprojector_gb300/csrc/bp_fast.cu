@@ -1827,7 +1827,7 @@ struct BatchUnit {
 // cost-sorted unit list with its own counters; a batch with both kinds runs the two
 // launches back to back.
 template <typename HT, bool CHECKED, bool PLANAR, bool FACT>
-__global__ void __launch_bounds__(288, 2)
+__global__ void __launch_bounds__(288, FACT ? kFactCtas : 3)
     bp_batch_kernel(const __grid_constant__ CUtensorMap tmap, const BatchCap *__restrict__ caps,
                     const BatchUnit *__restrict__ units, uint32_t n_units,
                     const float4 *__restrict__ tables, float *__restrict__ out,
@@ -1908,8 +1908,12 @@ struct BatchPlan {
     bool checked = false, planar = false;
     uint32_t n = 0, pitch = 0, stages = 0, chunk = 0, smem = 0, grid = 0, n_units = 0;
     // units [0, n_units - n_fact) run per-pair legs, the last n_fact factored legs (a
-    // second launch with grid_fact CTAs and the counters d_sched[2..3])
+    // second launch with grid_fact CTAs and the counters d_sched[2..3]); each launch has
+    // its own stage ring (ring[0] per-pair, ring[1] factored)
     uint32_t n_fact = 0, grid_fact = 0;
+    struct {
+        uint32_t chunk = 0, stages = 0, smem = 0;
+    } ring[2];
     uint32_t spin_limit = 1u << 22;
     uint64_t total_rows = 0, total_vox = 0, updates = 0;
     std::vector<uint64_t> row_off, vox_off;
@@ -1959,10 +1963,10 @@ int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
         void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
         void *args[] = {(void *)&map,         (void *)&b->d_caps, (void *)&units,
                         (void *)&nu,          (void *)&b->d_tables, (void *)&d_out,
-                        (void *)&b->d_diag,   (void *)&sched,     (void *)&b->stages,
+                        (void *)&b->d_diag,   (void *)&sched,     (void *)&b->ring[f].stages,
                         (void *)&b->spin_limit};
         BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(f ? b->grid_fact : b->grid), dim3(288), args,
-                                       b->smem, s));
+                                       b->ring[f].smem, s));
         count_launches(1);
     }
     b->last_stream = s;
@@ -2086,38 +2090,63 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         batch_free(b);
         return set_error(BPGB_ERR_UNSUPPORTED, "batch has too many rows for TMA coordinates");
     }
-    // common stage ring: the widest window sets the row slot
-    uint32_t chunk = o.chunk > 0 ? std::min<uint32_t>((uint32_t)o.chunk, kMaxChunk) : cfg.chunk;
-    uint32_t stages = o.stages > 0 ? std::min<uint32_t>((uint32_t)o.stages, 8) : cfg.stages;
-    stages = std::max<uint32_t>(stages, 2);
-    auto stage_bytes = [&](uint32_t ch) { return table_bytes_of(ch) + ch * max_row_bytes; };
-    if (o.stages <= 0)
-        while (stages > 2 && stages * stage_bytes(chunk) > 110 * 1024) stages--;
-    if (o.chunk <= 0)
-        while (chunk > 4 && stages * stage_bytes(chunk) > 110 * 1024) chunk = (chunk + 1) / 2;
-    while (chunk > 1 && stages * stage_bytes(chunk) > 200 * 1024) chunk = (chunk + 1) / 2;
-    if (stages * stage_bytes(chunk) > 200 * 1024) {
+    // One stage ring per launch: the widest window among that launch's captures sets its
+    // row slot.  The per-pair launch targets three CTAs per SM (72 KB of shared memory
+    // each), the factored one two (110 KB); factored captures need whole 4-SPAD blocks per
+    // stage and run per pair (their wider windows serve that form too) when their ring
+    // cannot hold them.
+    auto ring_of = [&](int f, uint32_t row_bytes, uint32_t *chunk_out, uint32_t *stages_out) {
+        uint32_t chunk = o.chunk > 0 ? std::min<uint32_t>((uint32_t)o.chunk, kMaxChunk) : cfg.chunk;
+        uint32_t stages = o.stages > 0 ? std::min<uint32_t>((uint32_t)o.stages, 8) : cfg.stages;
+        stages = std::max<uint32_t>(stages, 2);
+        const uint32_t soft = f ? 110 * 1024 : 72 * 1024;
+        auto sb = [&](uint32_t ch) { return table_bytes_of(ch) + ch * row_bytes; };
+        if (o.stages <= 0)
+            while (stages > 2 && stages * sb(chunk) > soft) stages--;
+        if (o.chunk <= 0)
+            while (chunk > 4 && stages * sb(chunk) > soft) chunk = (chunk + 1) / 2;
+        while (chunk > 1 && stages * sb(chunk) > 200 * 1024) chunk = (chunk + 1) / 2;
+        if (f) chunk = chunk / kFactS * kFactS;
+        *chunk_out = chunk;
+        *stages_out = stages;
+        return chunk > 0 && stages * sb(chunk) <= 200 * 1024;
+    };
+    uint32_t row_bytes[2] = {0, 0};
+    for (uint32_t c = 0; c < n; c++)
+        row_bytes[hc[c].a.fact ? 1 : 0] = std::max(row_bytes[hc[c].a.fact ? 1 : 0], hc[c].a.row_bytes);
+    uint32_t chunk[2] = {0, 0}, stages[2] = {0, 0};
+    if (row_bytes[1] && !ring_of(1, row_bytes[1], &chunk[1], &stages[1])) {
+        for (uint32_t c = 0; c < n; c++) hc[c].a.fact = 0;
+        row_bytes[0] = std::max(row_bytes[0], row_bytes[1]);
+        row_bytes[1] = 0;
+    }
+    if (row_bytes[0] && !ring_of(0, row_bytes[0], &chunk[0], &stages[0])) {
         batch_free(b);
         return set_error(BPGB_ERR_UNSUPPORTED, "widest time window does not fit in shared memory");
     }
-    b->chunk = chunk;
-    b->stages = stages;
-    b->smem = stages * stage_bytes(chunk) + 128;
+    for (int f = 0; f < 2; f++) {
+        b->ring[f].chunk = chunk[f];
+        b->ring[f].stages = stages[f];
+        b->ring[f].smem =
+            row_bytes[f] ? stages[f] * (table_bytes_of(chunk[f]) + chunk[f] * row_bytes[f]) + 128 : 0;
+    }
+    const int shown = row_bytes[0] ? 0 : 1;  // the ring bpgb_batch_info reports
+    b->chunk = chunk[shown];
+    b->stages = stages[shown];
+    b->smem = b->ring[shown].smem;
     b->planar = planar;
     b->pitch = (tmax + bw - 1) / bw * bw;
     std::vector<BatchUnit> units;
     std::vector<uint64_t> cost;
     for (uint32_t c = 0; c < n; c++) {
         FastArgs &a = hc[c].a;
-        a.chunk = chunk;
-        a.stages = stages;
-        a.table_bytes = table_bytes_of(chunk);
-        a.stage_bytes = stage_bytes(chunk);
-        // factored captures need whole 4-SPAD blocks per stage; their (wider) windows
-        // serve the per-pair form as well
-        if (chunk % kFactS) a.fact = 0;
-        a.nchunks = a.fact ? (uint32_t)((a.L + chunk / kFactS - 1) / (chunk / kFactS))
-                           : (uint32_t)((a.S + chunk - 1) / chunk);
+        const int f = a.fact ? 1 : 0;
+        a.chunk = chunk[f];
+        a.stages = stages[f];
+        a.table_bytes = table_bytes_of(chunk[f]);
+        a.stage_bytes = table_bytes_of(chunk[f]) + chunk[f] * row_bytes[f];
+        a.nchunks = a.fact ? (uint32_t)((a.L + chunk[f] / kFactS - 1) / (chunk[f] / kFactS))
+                           : (uint32_t)((a.S + chunk[f] - 1) / chunk[f]);
         if (fast_items(a) >= (1ull << 32)) {
             batch_free(b);
             return set_error(BPGB_ERR_UNSUPPORTED, "more than 2^32 (laser, chunk) items");
@@ -2148,12 +2177,12 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         const uint32_t nu = f ? b->n_fact : b->n_units - b->n_fact;
         if (!nu) continue;
         void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
-        if (int rs = reserve_dynamic_smem(kern, b->smem)) {
+        if (int rs = reserve_dynamic_smem(kern, b->ring[f].smem)) {
             batch_free(b);
             return rs;
         }
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 288, b->smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 288, b->ring[f].smem);
         if (e != cudaSuccess || occ < 1) {
             batch_free(b);
             return e != cudaSuccess ? cuda_error(e, "batch kernel attributes")
