@@ -549,7 +549,6 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
     uint32_t cur_l = ~0u;
     uint32_t violations = 0;
     const float2 magic2 = make_float2(kMagic, kMagic);
-    const uint32_t row_elems = a.row_bytes / esz;
 
     uint32_t stage = (uint32_t)(step0 % a.stages);
     uint32_t phase = (uint32_t)(step0 / a.stages) & 1;
@@ -652,7 +651,6 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
 #pragma unroll
             for (int p = 0; p < NP; p++) acc[p].fold(comp[p], part[p]);
         }
-        (void)row_elems;
         if (++stage == a.stages) stage = 0, phase ^= 1;
         if (++c == a.nchunks) c = 0, l++;
     }
