@@ -1814,10 +1814,11 @@ struct BatchCap {
     uint64_t row_base;  // first row of the capture in the packed H
     uint64_t out_off;   // first voxel of the capture in the packed output
     uint64_t tab_off;   // first table entry (SPADs then lasers)
+    uint64_t part_off;  // a.splits > 1: first float of its split-major partial sums in scratch
 };
 
 struct BatchUnit {
-    uint32_t cap, tile;
+    uint32_t cap, tile, split;
 };
 
 // FACT: the launch over the batch's lasers x SPADs captures (factored legs); otherwise the
@@ -1829,8 +1830,8 @@ __global__ void __launch_bounds__(288, FACT ? kFactCtas : 3)
     bp_batch_kernel(const __grid_constant__ CUtensorMap tmap, const BatchCap *__restrict__ caps,
                     const BatchUnit *__restrict__ units, uint32_t n_units,
                     const float4 *__restrict__ tables, float *__restrict__ out,
-                    unsigned long long *__restrict__ diag, unsigned int *__restrict__ sched,
-                    uint32_t stages, uint32_t spin_limit) {
+                    float *__restrict__ scratch, unsigned long long *__restrict__ diag,
+                    unsigned int *__restrict__ sched, uint32_t stages, uint32_t spin_limit) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[8];
     __shared__ __align__(8) uint64_t empty_bar[8];
@@ -1861,12 +1862,14 @@ __global__ void __launch_bounds__(288, FACT ? kFactCtas : 3)
         __syncthreads();
         if (*(volatile int *)&abort_flag) break;
         const float4 *tab = tables + cap_s.tab_off;
+        // split captures write partial sums (reduced after the launch), the rest the volume
+        float *dst = cap_s.a.splits > 1 ? scratch + cap_s.part_off : out + cap_s.out_off;
         if constexpr (FACT)
-            ok = fact_unit<HT, CHECKED>(cap_s.a, &tmap, tab, tab + cap_s.a.S, out + cap_s.out_off,
-                                        diag, u.tile, 0, (uint32_t)cap_s.row_base, step, sh);
+            ok = fact_unit<HT, CHECKED>(cap_s.a, &tmap, tab, tab + cap_s.a.S, dst, diag, u.tile,
+                                        u.split, (uint32_t)cap_s.row_base, step, sh);
         else
             ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows>(
-                cap_s.a, &tmap, tab, tab + cap_s.a.S, out + cap_s.out_off, diag, u.tile, 0,
+                cap_s.a, &tmap, tab, tab + cap_s.a.S, dst, diag, u.tile, u.split,
                 (uint32_t)cap_s.row_base, step, sh);
         if (!ok) *(volatile int *)&abort_flag = 1;
     }
@@ -1912,6 +1915,16 @@ struct BatchPlan {
     struct {
         uint32_t chunk = 0, stages = 0, smem = 0;
     } ring[2];
+    // captures whose units are split over pair ranges: partial sums in d_scratch, added
+    // into the volume after their launch
+    struct Split {
+        int fact;
+        uint32_t splits;
+        uint64_t part_off, out_off, nvox;
+        float scale;
+    };
+    std::vector<Split> splits;
+    float *d_scratch = nullptr;
     uint32_t spin_limit = 1u << 22;
     uint64_t total_rows = 0, total_vox = 0, updates = 0;
     std::vector<uint64_t> row_off, vox_off;
@@ -1936,6 +1949,7 @@ void batch_free(BatchPlan *b) {
     cudaFree(b->d_tables);
     cudaFree(b->d_diag);
     cudaFree(b->d_sched);
+    cudaFree(b->d_scratch);
     delete b;
 }
 
@@ -1959,13 +1973,21 @@ int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
         const BatchUnit *units = b->d_units + (f ? n_pp : 0);
         unsigned int *sched = b->d_sched + (f ? 2 : 0);
         void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
-        void *args[] = {(void *)&map,         (void *)&b->d_caps, (void *)&units,
-                        (void *)&nu,          (void *)&b->d_tables, (void *)&d_out,
-                        (void *)&b->d_diag,   (void *)&sched,     (void *)&b->ring[f].stages,
-                        (void *)&b->spin_limit};
+        void *args[] = {(void *)&map,         (void *)&b->d_caps,    (void *)&units,
+                        (void *)&nu,          (void *)&b->d_tables,  (void *)&d_out,
+                        (void *)&b->d_scratch, (void *)&b->d_diag,   (void *)&sched,
+                        (void *)&b->ring[f].stages, (void *)&b->spin_limit};
         BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(f ? b->grid_fact : b->grid), dim3(288), args,
                                        b->ring[f].smem, s));
         count_launches(1);
+        for (const auto &sp : b->splits) {  // partial sums of this launch's split captures
+            if (sp.fact != f) continue;
+            const unsigned blocks = (unsigned)std::min<uint64_t>((sp.nvox + 255) / 256, 152ull * 8);
+            reduce_splits_kernel<false, false><<<blocks, 256, 0, s>>>(
+                b->d_scratch + sp.part_off, d_out + sp.out_off, sp.nvox, sp.splits, sp.scale);
+            count_launches(1);
+        }
+        BPGB_CUDA_TRY(cudaGetLastError());
     }
     b->last_stream = s;
     return BPGB_OK;
@@ -2134,8 +2156,6 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     b->smem = b->ring[shown].smem;
     b->planar = planar;
     b->pitch = (tmax + bw - 1) / bw * bw;
-    std::vector<BatchUnit> units;
-    std::vector<uint64_t> cost;
     for (uint32_t c = 0; c < n; c++) {
         FastArgs &a = hc[c].a;
         const int f = a.fact ? 1 : 0;
@@ -2150,30 +2170,12 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
             return set_error(BPGB_ERR_UNSUPPORTED, "more than 2^32 (laser, chunk) items");
         }
         a.planar = planar ? 1 : 0;
-        const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
-        for (uint64_t t = 0; t < ntiles; t++) units.push_back({c, (uint32_t)t});
     }
-    // longest units first (pairs x tile voxels), stable within a capture
-    std::vector<uint32_t> order(units.size());
-    for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
-    auto unit_cost = [&](const BatchUnit &u) {
-        const FastArgs &a = hc[u.cap].a;
-        return (uint64_t)a.L * a.S * a.tdim[0] * a.tdim[1] * a.tdim[2];
-    };
-    // per-pair units first, then the factored ones; each list longest first
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-        const bool fx = hc[units[x].cap].a.fact != 0, fy = hc[units[y].cap].a.fact != 0;
-        if (fx != fy) return fy;
-        return unit_cost(units[x]) > unit_cost(units[y]);
-    });
-    std::vector<BatchUnit> sorted(units.size());
-    for (size_t i = 0; i < order.size(); i++) sorted[i] = units[order[i]];
-    b->n_units = (uint32_t)sorted.size();
-    for (const BatchUnit &u : sorted) b->n_fact += hc[u.cap].a.fact ? 1 : 0;
+    // resident CTAs of each launch
     cudaError_t e = cudaSuccess;
+    uint64_t resident[2] = {0, 0};
     for (int f = 0; f < 2; f++) {
-        const uint32_t nu = f ? b->n_fact : b->n_units - b->n_fact;
-        if (!nu) continue;
+        if (!row_bytes[f]) continue;
         void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
         if (int rs = reserve_dynamic_smem(kern, b->ring[f].smem)) {
             batch_free(b);
@@ -2186,8 +2188,62 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
             return e != cudaSuccess ? cuda_error(e, "batch kernel attributes")
                                     : set_error(BPGB_ERR_UNSUPPORTED, "batch kernel does not fit on an SM");
         }
-        (f ? b->grid_fact : b->grid) = (uint32_t)std::min<uint64_t>(nu, (uint64_t)sms * occ);
+        resident[f] = (uint64_t)sms * occ;
     }
+    // Units are (capture, tile, pair range).  A capture whose (capture, tile) unit is long
+    // against a resident CTA's share of its launch is split into up to 8 pair ranges, so
+    // the launch ends evenly (greedy longest-first over many short units); its ranges
+    // write partial sums that are added, in range order, after the launch.
+    auto unit_cost = [&](uint32_t c) {
+        const FastArgs &a = hc[c].a;
+        return (double)a.L * a.S * a.tdim[0] * a.tdim[1] * a.tdim[2];
+    };
+    double share[2] = {0.0, 0.0};
+    for (uint32_t c = 0; c < n; c++) {
+        const FastArgs &a = hc[c].a;
+        share[a.fact ? 1 : 0] += unit_cost(c) * a.tiles[0] * a.tiles[1] * a.tiles[2];
+    }
+    for (int f = 0; f < 2; f++)
+        if (resident[f]) share[f] /= (double)resident[f];
+    uint64_t scratch = 0;
+    std::vector<BatchUnit> units;
+    for (uint32_t c = 0; c < n; c++) {
+        FastArgs &a = hc[c].a;
+        const int f = a.fact ? 1 : 0;
+        const double target = share[f] / 24.0;  // unit length aimed at
+        uint64_t sp = target > 0.0 ? (uint64_t)std::llround(unit_cost(c) / target) : 1;
+        sp = std::max<uint64_t>(1, std::min<uint64_t>({sp, 8, fast_items(a)}));
+        if (o.pair_splits > 0) sp = std::min<uint64_t>((uint64_t)o.pair_splits, fast_items(a));
+        a.splits = (uint32_t)sp;
+        hc[c].part_off = scratch;
+        if (sp > 1) {
+            b->splits.push_back({f, (uint32_t)sp, scratch, hc[c].out_off, a.nvox, a.out_scale});
+            scratch += sp * a.nvox;
+        }
+        const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+        for (uint32_t k = 0; k < sp; k++)
+            for (uint64_t t = 0; t < ntiles; t++) units.push_back({c, (uint32_t)t, k});
+    }
+    // per-pair units first, then the factored ones; each list longest first
+    std::vector<uint32_t> order(units.size());
+    for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
+    auto cost_of = [&](const BatchUnit &u) { return unit_cost(u.cap) / hc[u.cap].a.splits; };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const bool fx = hc[units[x].cap].a.fact != 0, fy = hc[units[y].cap].a.fact != 0;
+        if (fx != fy) return fy;
+        return cost_of(units[x]) > cost_of(units[y]);
+    });
+    std::vector<BatchUnit> sorted(units.size());
+    for (size_t i = 0; i < order.size(); i++) sorted[i] = units[order[i]];
+    if (sorted.size() >= (1ull << 32)) {
+        batch_free(b);
+        return set_error(BPGB_ERR_UNSUPPORTED, "too many work units");
+    }
+    b->n_units = (uint32_t)sorted.size();
+    for (const BatchUnit &u : sorted) b->n_fact += hc[u.cap].a.fact ? 1 : 0;
+    b->grid = (uint32_t)std::min<uint64_t>(b->n_units - b->n_fact, resident[0]);
+    b->grid_fact = (uint32_t)std::min<uint64_t>(b->n_fact, resident[1]);
+    if (scratch) e = cudaMalloc(&b->d_scratch, scratch * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_caps, n * sizeof(BatchCap));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_units, sorted.size() * sizeof(BatchUnit));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4));

@@ -93,9 +93,9 @@ def test_batch_matches_plans_and_oracle(cuda, dtype):
 
 @pytest.mark.parametrize("frac", [0.0, 1.0])
 def test_batch_of_one_kind(cuda, frac):
-    """Only single-laser captures (one launch, per-pair legs) or only lasers x SPADs
-    captures (one launch, factored legs); the unfactored option runs every capture per
-    pair."""
+    """Only single-laser captures (one persistent launch, per-pair legs) or only lasers x
+    SPADs captures (one persistent launch, factored legs); the unfactored option runs every
+    capture per pair."""
     import torch
 
     caps = small_batch(n=5, seed=6, exhaustive_frac=frac)
@@ -107,7 +107,8 @@ def test_batch_of_one_kind(cuda, frac):
             launches = capi.launch_count()
             b.execute(dH, dV)
             torch.cuda.synchronize()
-            assert capi.launch_count() - launches == 1
+            # one persistent launch, plus one reduction per capture split over pair ranges
+            assert 1 <= capi.launch_count() - launches <= 1 + len(caps)
             assert b.check() == 0
             outs.append(volumes(caps, b, dV.cpu().numpy()))
     for i, c in enumerate(caps):
@@ -116,6 +117,25 @@ def test_batch_of_one_kind(cuda, frac):
             assert oracle.rel_l2(vols[i], ref) < tol(c), i
         if frac == 0.0:  # nothing to factor: both runs are the same launch
             assert np.array_equal(outs[0][i], outs[1][i])
+
+
+@pytest.mark.parametrize("splits", [1, 3])
+def test_batch_pair_splits_option(cuda, splits):
+    """Every capture's units split over `splits` pair ranges (partial sums added after the
+    launch in range order) or none: the same volumes within summation order."""
+    caps = small_batch(n=6, seed=7)
+    geo = synthetic.batch_geometry(caps)
+    outs = []
+    for sp in (splits, 0):
+        with capi.Batch(geo, h_dtype=capi.DTYPE_F32, checked=1, pair_splits=sp) as b:
+            H, dH, dV = upload(cuda, caps, b, np.float32, None)
+            b.execute(dH, dV)
+            assert b.check() == 0
+            outs.append(volumes(caps, b, dV.cpu().numpy()))
+    for i, c in enumerate(caps):
+        assert oracle.rel_l2(outs[0][i], outs[1][i]) < 1e-6, i
+        ref = oracle.bp_gpu_f64(c.H, c.pairs, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT)
+        assert oracle.rel_l2(outs[0][i], ref) < tol(c), i
 
 
 def test_batch_graph_replays_and_recaptures(cuda):
