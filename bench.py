@@ -591,6 +591,13 @@ def run_batch(args):
         step()
     stream.synchronize()
     batch.check()
+    # kernels one batch execute launches (persistent launches + split reductions): the
+    # captured graph replays exactly these
+    k0 = capi.launch_count()
+    batch.execute(dH, dV, stream)
+    stream.synchronize()
+    per_step = capi.launch_count() - k0
+    batch.check()
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -604,8 +611,9 @@ def run_batch(args):
         e1.record(stream)
         e1.synchronize()
     torch.cuda.synchronize()
-    # graph replays launch the captured kernel once each; the capture itself counted one
-    launches = max(capi.launch_count() - launches0, 0) + args.steps
+    # graph replays launch the captured kernels without passing through the library's
+    # counter: per_step kernels each
+    launches = max(capi.launch_count() - launches0, 0) + per_step * args.steps
     ms = e0.elapsed_time(e1) / args.steps
     batch.check()
     ms = max_over_ranks(ms, dev)
