@@ -224,19 +224,23 @@ int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h_pitch,
                              const float *volume_zero_pos, const float *voxel_inc, float t0,
                              float deltaT, float *d_volume, void *stream);
 
-/* ---- batches: many captures in one persistent launch ---------------------------
+/* ---- batches: many captures in persistent launches ------------------------------
  * No counterpart in the reference (it reconstructs one capture per call and relaunches
  * a 16^3 grid per 4096 voxels).  A batch holds the geometry of n captures of uneven pair
  * grids, T and volumes.  Their rows are packed into ONE device buffer
  * [total_rows, pitch] (capture c starts at row_offsets[c]; bins T_c..pitch-1 must be
  * zero) of opt->h_dtype (FP32 or FP16; per-capture h_scale multiplies the result), and
  * their volumes into one float buffer (capture c at voxel_offsets[c]).  execute runs
- * every voxel tile of every capture in one persistent kernel, longest tiles first, each
- * CTA taking the next tile from a device work counter that the launch re-arms when it
- * ends; graph_launch captures that launch in a CUDA graph once per (d_H, d_volumes)
- * pair and replays it.  Launches of ONE batch must not overlap (stream-order them):
- * they share the work counter.  Each capture's pairs must factor as lasers x SPADs or
- * be confocal. */
+ * every work unit -- (capture, voxel tile, pair range) -- in persistent kernels, longest
+ * units first, each CTA taking the next unit from a device work counter that the launch
+ * re-arms when it ends: one launch for the captures with per-pair legs, one for the
+ * lasers x SPADs captures with factored legs (opt->unfactored = 1: all per pair), then one
+ * reduction per capture whose tiles were split over pair ranges (opt->pair_splits > 0
+ * fixes the ranges per capture; 0 chooses them from each unit's length against a CTA's
+ * share of its launch).  graph_launch captures these launches in a CUDA graph once per
+ * (d_H, d_volumes) pair and replays it.  Executes of ONE batch must not overlap
+ * (stream-order them): they share the work counters and the partial-sum scratch.  Each
+ * capture's pairs must factor as lasers x SPADs or be confocal. */
 typedef struct bpgb_capture_geometry {
     const bpgb_pair *pairs; /* host pair list of the capture */
     uint64_t num_pairs;
@@ -253,9 +257,9 @@ typedef struct bpgb_batch_info {
     uint32_t pitch;       /* elements per packed row */
     uint64_t total_rows;  /* rows of the packed H */
     uint64_t total_voxels;
-    uint32_t work_units;  /* voxel tiles over all captures */
-    uint32_t grid;        /* persistent CTAs */
-    uint32_t stages, chunk, smem_bytes;
+    uint32_t work_units;  /* (capture, voxel tile, pair range) units over all captures */
+    uint32_t grid;        /* persistent CTAs of the larger launch */
+    uint32_t stages, chunk, smem_bytes; /* the per-pair launch's ring (else the factored) */
     uint64_t updates;     /* voxel x pair updates per execute */
     int32_t planar;       /* the planar-wall kernel variant runs */
 } bpgb_batch_info;
