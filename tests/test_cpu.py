@@ -49,6 +49,23 @@ def test_abi_version_and_status_strings():
     assert o.algo == capi.ALGO_AUTO and o.h_scale == 1.0 and o.tile == -1
 
 
+def test_options_mirror_matches_the_c_struct():
+    """bpgb_options_default writes exactly the mirrored bytes: a sentinel right after the
+    ctypes Options stays untouched, and the defaults land in the named fields."""
+    import ctypes as C
+
+    class Guarded(C.Structure):
+        _fields_ = [("o", capi.Options), ("guard", C.c_uint8 * 64)]
+
+    g = Guarded()
+    C.memset(C.byref(g), 0xAB, C.sizeof(g))
+    capi.lib().bpgb_options_default(C.byref(g.o))
+    assert bytes(g.guard) == b"\xab" * 64
+    assert g.o.unfactored == 0 and list(g.o.reserved) == [0, 0, 0, 0]
+    assert g.o.h_dtype == capi.DTYPE_F32 and g.o.accum == capi.ACCUM_F32
+    assert C.sizeof(capi.Options) == 16 * 4
+
+
 def test_volume_basis_axis_aligned_and_wall_normal():
     zero, inc = capi.volume_basis((0, 1, 0), (1, 2, 3), (11, 21, 31))
     assert np.allclose(zero, [-0.5, 0.0, -1.5])
