@@ -137,6 +137,21 @@ def cpu_baseline(cap, sample_voxels: int, seed: int = 0):
     return len(ids) * cap.P / dt, dt, len(ids), oracle.num_threads()
 
 
+def cpu_sample_for(rate: float, pairs: int, seconds: float, lo: int, hi: int) -> int:
+    """Voxels a CPU sample needs to last about `seconds` at `rate` updates/s."""
+    return int(min(hi, max(lo, seconds * rate / max(pairs, 1))))
+
+
+def cpu_baseline_timed(cap, seconds: float, probe: int, seed: int = 0):
+    """cpu_baseline on a sample sized to about `seconds` of CPU work (a `probe`-voxel run
+    calibrates the rate first)."""
+    r, dt, n, cores = cpu_baseline(cap, probe, seed)
+    want = cpu_sample_for(r, cap.P, seconds, probe, cap.nvox)
+    if want > n:
+        r, dt, n, cores = cpu_baseline(cap, want, seed)
+    return r, dt, n, cores
+
+
 def run_reference_arm(args):
     """--impl reference: the reference's CPU implementation of the path on host cores."""
     ws, rank, _ = dist_env()
@@ -148,15 +163,18 @@ def run_reference_arm(args):
         return run_reference_arm_batch(args)
     name = "octree_256" if args.workload == "octree_256_learned" else args.workload
     cap = synthetic.make_capture(name, seed=args.seed)
+    # each step: a seeded voxel sample sized (during warm-up) to about --ref-seconds
+    sample = args.ref_sample
     for _ in range(args.warmup):
-        cpu_baseline(cap, args.ref_sample, seed=1)
-    rates, secs = [], []
+        r, _, _, _ = cpu_baseline(cap, sample, seed=1)
+        sample = cpu_sample_for(r, cap.P, args.ref_seconds, args.ref_sample, cap.nvox)
+    secs = []
     cores = None
     for k in range(args.steps):
-        r, dt, n, cores = cpu_baseline(cap, args.ref_sample, seed=100 + k)
-        rates.append(r)
+        r, dt, n, cores = cpu_baseline(cap, sample, seed=100 + k)
         secs.append(dt)
-    value = float(np.sum([args.ref_sample * cap.P for _ in rates]) / np.sum(secs))
+    value = float(sample * cap.P * args.steps / np.sum(secs))
+    args.ref_sample = sample
     line = {
         "impl": "reference", "metric": "voxel-pair updates/s", "value": value, "unit": "updates/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -181,7 +199,9 @@ def run_reference_arm_batch(args):
     caps = synthetic.make_batch(64, seed=args.seed)
     per = max(1, args.ref_sample // 4)
     for _ in range(args.warmup):
-        cpu_baseline_batch(caps, per, seed=1)
+        r, _, _, _ = cpu_baseline_batch(caps, per, seed=1)
+        per = cpu_sample_for(r, sum(c.P for c in caps), args.ref_seconds,
+                             max(1, args.ref_sample // 4), min(c.nvox for c in caps))
     upd, secs, cores = 0.0, [], None
     for k in range(args.steps):
         r, dt, _, cores = cpu_baseline_batch(caps, per, seed=100 + k)
@@ -357,7 +377,7 @@ def run_ours(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        r, dt, nvs, cores = cpu_baseline(cap, args.cpu_sample)
+        r, dt, nvs, cores = cpu_baseline_timed(cap, args.cpu_seconds, args.cpu_sample)
         line["cpu_baseline"] = {"value": r, "unit": "updates/s", "cores": cores, "kind": "port",
                                 "sample": f"{nvs} seeded random voxels x all {cap.P} pairs "
                                           f"({dt:.1f} s); reference classic_backprojection "
@@ -691,7 +711,12 @@ def run_batch(args):
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        r, dt, nvs, cores = cpu_baseline_batch(caps, max(1, args.cpu_sample // 64))
+        probe = max(1, args.cpu_sample // 64)
+        r, dt, nvs, cores = cpu_baseline_batch(caps, probe)
+        per = cpu_sample_for(r, sum(c.P for c in caps), args.cpu_seconds, probe,
+                             min(c.nvox for c in caps))
+        if per > nvs:
+            r, dt, nvs, cores = cpu_baseline_batch(caps, per)
         line["cpu_baseline"] = {"value": r, "unit": "updates/s", "cores": cores, "kind": "port",
                                 "sample": f"{nvs} seeded random voxels of each of the 64 "
                                           f"captures x all their pairs ({dt:.1f} s); reference "
@@ -714,10 +739,10 @@ def cpu_baseline_batch(caps, per_capture: int, seed: int = 0):
 
 
 def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored=0.0):
-    """factored: the fraction of the updates that run the factored lasers x SPADs body
-    (1.0 for a factored plan); the peak blends the two bodies' peaks by their updates."""
     """Roofline of the FAST kernels: per-update pipe work against the pipe rates measured
-    on this GPU, at the median SM clock of the timed region."""
+    on this GPU, at the median SM clock of the timed region.  factored: the fraction of the
+    updates that run the factored lasers x SPADs body (1.0 for a factored plan); the peak
+    blends the two bodies' peaks by their updates."""
     import torch
 
     from backprojector_gb300 import capi
@@ -791,8 +816,14 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--voxels", type=int, default=None,
                     help="override the volume resolution (reduced profiling cases)")
-    ap.add_argument("--cpu-sample", type=int, default=1024)
-    ap.add_argument("--ref-sample", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=1024,
+                    help="voxels of the calibration run of the CPU baseline")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU work the cpu_baseline sample is sized to")
+    ap.add_argument("--ref-sample", type=int, default=256,
+                    help="smallest per-step voxel sample of --impl reference")
+    ap.add_argument("--ref-seconds", type=float, default=1.0,
+                    help="CPU work per step --impl reference sizes its sample to")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ref-gpu", action="store_true", help="accepted for compatibility")
     args = ap.parse_args()
