@@ -469,7 +469,8 @@ def phasor_pulse_device(d_H, rows: int, T: int, in_pitch: int, wavelength: float
 
 class Batch:
     """bpgb_batch: many captures (list of dicts or Capture-like objects with pairs, T,
-    voxels_per_side, zero, inc, t0, deltaT and optional h_scale) in one persistent launch.
+    voxels_per_side, zero, inc, t0, deltaT and optional h_scale) in persistent launches
+    (one per kind of capture) captured together in one CUDA graph.
 
     Device buffers: H packed [total_rows, pitch] (capture c at rows row_offsets[c], bins
     >= its T zero) and volumes packed [total_voxels] (capture c at voxel_offsets[c])."""

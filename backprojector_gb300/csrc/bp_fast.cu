@@ -1796,16 +1796,19 @@ void fast_plan_free(FastPlan *fp) {
 }
 
 // ==================================================================================
-// Batches: many captures of uneven grids, T and volumes in ONE persistent launch.
+// Batches: many captures of uneven grids, T and volumes in persistent launches.
 //
 // All captures' rows live in one packed device buffer [sum P_c, pitch] (capture c at
 // rows row_base_c; bins T_c..pitch zero) behind a single TMA tensor map whose box width
-// is shared.  Each capture has a launch descriptor (FastArgs, table and output offsets)
-// in device memory.  The work list holds one (capture, tile) unit per voxel tile, sorted
-// by cost (pairs x tile voxels) in decreasing order; each CTA takes the next unit from
+// is shared.  Each capture has a launch descriptor (FastArgs, table, output and partial-sum
+// offsets) in device memory.  The work lists hold (capture, tile, pair range) units, one
+// list per launch (per-pair legs; factored lasers x SPADs legs), each sorted by cost
+// (pairs x tile voxels / ranges) in decreasing order; each CTA takes the next unit from
 // an atomic counter when it finishes one (greedy longest-first), with its pipeline (stage
-// ring, mbarrier phases) continuing across units.  The launch allocates nothing, so a caller can capture it in a CUDA graph;
-// bpgb_batch_graph_launch does that once per buffer pair and replays the graph.
+// ring, mbarrier phases) continuing across units.  Captures split over pair ranges write
+// partial sums that a reduction adds after their launch.  The launches allocate nothing,
+// so a caller can capture them in a CUDA graph; bpgb_batch_graph_launch does that once per
+// buffer pair and replays the graph.
 // ==================================================================================
 namespace {
 
