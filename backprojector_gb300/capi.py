@@ -126,6 +126,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "bpgb_plan_get_info": (C.c_int, [_P, C.POINTER(PlanInfo)]),
     "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
+    "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "bpgb_plan_destroy": (C.c_int, [_P]),
     "bpgb_diag_wait_timeout": (C.c_int, [C.c_uint32]),
     "bpgb_diag_pipe_rates": (C.c_int, [C.POINTER(C.c_double)]),
@@ -442,6 +443,15 @@ class Plan:
         check(lib().bpgb_plan_dump_bins(self.handle, ids.ctypes.data_as(C.POINTER(C.c_int64)),
                                         len(ids), _ptr(d_bins), _stream_ptr(stream)),
               "bpgb_plan_dump_bins")
+
+    def tables(self) -> np.ndarray:
+        """The FAST plan's tables as float32 [S + L, 4] (SPAD entries, then lasers)."""
+        n = C.c_uint64(0)
+        check(lib().bpgb_plan_get_tables(self.handle, None, 0, C.byref(n)), "bpgb_plan_get_tables")
+        out = np.zeros((int(n.value), 4), np.float32)
+        check(lib().bpgb_plan_get_tables(self.handle, out.ctypes.data_as(C.c_void_p), n.value,
+                                         C.byref(n)), "bpgb_plan_get_tables")
+        return out
 
     def close(self) -> None:
         if getattr(self, "handle", None):

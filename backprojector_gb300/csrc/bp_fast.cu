@@ -60,6 +60,7 @@ constexpr int kC64Rows = 1;    // already double the registers
 constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
 constexpr uint32_t kFactS = 4;  // SPADs per block of the factored lasers x SPADs form
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
+constexpr uint32_t kPlanDiagWords = 8;  // a plan's device counters (see fast_plan_build)
 // row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
 __host__ __device__ constexpr uint32_t table_bytes_of(uint32_t c) {
     return (c * kRecordBytes + 127) / 128 * 128;
@@ -1169,6 +1170,116 @@ __global__ void wait_timeout_probe_kernel(uint32_t limit, unsigned long long *ou
     if (threadIdx.x == 0) out[0] = ok ? 0ull : 1ull;
 }
 
+// ---- FP64 tables of the FAST kernels, built on the GPU --------------------------------
+// SPAD entry s: (frame position relative to the volume origin, cw / dT) -- (cw + lw) / dT
+// when confocal; laser entry l: (frame position, lw / dT - t0 / dT).  The pair precompute
+// of the reference keeps its wall legs in double (backproject.hpp:356-418); these are the
+// values the kernels' FP32 arithmetic starts from, formed in FP64 with every operation
+// rounded separately (no contraction) in a fixed order.
+struct TableArgs {
+    double u[3][3];  // orthonormal frame rows of the voxel basis
+    double zero[3];
+    double dT, t0;
+    uint64_t L, S;
+    int confocal;
+    uint32_t kax;  // voxel-line axis of the tile preset (planar-wall test)
+};
+
+__device__ __forceinline__ void frame_fp64(const TableArgs &t, const float *pt, double o[3]) {
+    const double d0 = __dsub_rn((double)pt[0], t.zero[0]);
+    const double d1 = __dsub_rn((double)pt[1], t.zero[1]);
+    const double d2 = __dsub_rn((double)pt[2], t.zero[2]);
+    for (int r = 0; r < 3; r++)
+        o[r] = __dadd_rn(__dadd_rn(__dmul_rn(t.u[r][0], d0), __dmul_rn(t.u[r][1], d1)),
+                         __dmul_rn(t.u[r][2], d2));
+}
+
+__device__ __forceinline__ bool same_point(const float *a, const float *b) {
+    return __float_as_uint(a[0]) == __float_as_uint(b[0]) &&
+           __float_as_uint(a[1]) == __float_as_uint(b[1]) &&
+           __float_as_uint(a[2]) == __float_as_uint(b[2]);
+}
+
+// Tables (S SPAD entries, then L laser entries) from a device pair list in the order
+// p = l * S + s (or confocal), with three checks counted in diag: diag[0] pairs that
+// break that order, diag[1] non-finite pair values, diag[2] SPADs whose FP32 frame
+// coordinate along kax differs from SPAD 0's (0 = planar wall for that axis).
+__global__ void tables_fp64_kernel(const bpgb_pair *__restrict__ pairs, const TableArgs t,
+                                   float4 *__restrict__ tab, unsigned long long *__restrict__ diag) {
+    __shared__ float g0k;  // SPAD 0's kax coordinate, formed once per block
+    if (threadIdx.x == 0) {
+        double g0[3];
+        frame_fp64(t, pairs[0].camera_point, g0);
+        g0k = (float)g0[t.kax];
+    }
+    __syncthreads();
+    const uint64_t P = t.L * t.S;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const bpgb_pair pr = pairs[p];
+        const uint64_t l = p / t.S, s = p % t.S;
+        const float *f = reinterpret_cast<const float *>(&pr);
+        bool finite = true;
+        for (int k = 0; k < 8; k++) finite = finite && isfinite(f[k]);
+        if (!finite) atomicAdd(&diag[1], 1ull);
+        bool ok;
+        if (t.confocal) {
+            ok = same_point(pr.laser_point, pr.camera_point) &&
+                 __float_as_uint(pr.laser_wall) == __float_as_uint(pr.camera_wall);
+        } else {
+            const bpgb_pair &head = pairs[l * t.S];
+            const bpgb_pair &col = pairs[s];
+            ok = same_point(pr.laser_point, head.laser_point) &&
+                 __float_as_uint(pr.laser_wall) == __float_as_uint(head.laser_wall) &&
+                 same_point(pr.camera_point, col.camera_point) &&
+                 __float_as_uint(pr.camera_wall) == __float_as_uint(col.camera_wall);
+        }
+        if (!ok) atomicAdd(&diag[0], 1ull);
+        if (l == 0) {
+            double g[3];
+            frame_fp64(t, pr.camera_point, g);
+            const double cs = t.confocal
+                                  ? __ddiv_rn(__dadd_rn((double)pr.camera_wall, (double)pr.laser_wall), t.dT)
+                                  : __ddiv_rn((double)pr.camera_wall, t.dT);
+            tab[s] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)cs);
+            if (__float_as_uint((float)g[t.kax]) != __float_as_uint(g0k)) atomicAdd(&diag[2], 1ull);
+        }
+        if (s == 0) {
+            double g[3] = {0.0, 0.0, 0.0};
+            double c = __ddiv_rn(-t.t0, t.dT);
+            if (!t.confocal) {
+                frame_fp64(t, pr.laser_point, g);
+                c = __dadd_rn(c, __ddiv_rn((double)pr.laser_wall, t.dT));
+            }
+            tab[t.S + l] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)c);
+        }
+    }
+}
+
+// Queues tables_fp64_kernel for L lasers x S SPADs (L = 1 when confocal) on stream s;
+// diag[0..2] must be zero beforehand.
+int launch_tables(const bpgb_pair *d_pairs, const Volume &vol, const double u[3][3], double dT,
+                  double t0, uint64_t L, uint64_t S, bool confocal, uint32_t kax, float4 *d_tab,
+                  unsigned long long *d_diag, int sms, cudaStream_t s) {
+    TableArgs ta{};
+    for (int r = 0; r < 3; r++)
+        for (int k = 0; k < 3; k++) ta.u[r][k] = u[r][k];
+    for (int k = 0; k < 3; k++) ta.zero[k] = (double)vol.zero[k];
+    ta.dT = dT;
+    ta.t0 = t0;
+    ta.L = L;
+    ta.S = S;
+    ta.confocal = confocal ? 1 : 0;
+    ta.kax = kax;
+    const uint64_t P = L * S;
+    const unsigned blocks = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((P + 255) / 256, (uint64_t)std::max(sms, 1) * 16));
+    tables_fp64_kernel<<<blocks, 256, 0, s>>>(d_pairs, ta, d_tab, d_diag);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
 // ---- tensor-map encoder from the driver (no libcuda link needed) -----------------
 using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                    const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -1441,11 +1552,9 @@ void *plan_kernel(const FastPlan *fp) {
                                     fp->wide);
 }
 
-int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
-                    uint64_t P, const Factorization &fz, const Volume &vol,
-                    const BinParams &bp, const bpgb_options &opt, int sm_count,
-                    std::string *why_not) {
-    (void)d_pairs;
+int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
+                    const Factorization &fz, const Volume &vol, const BinParams &bp,
+                    const bpgb_options &opt, int sm_count, std::string *why_not) {
     *out = nullptr;
     auto no = [&](const std::string &m) {
         if (why_not) *why_not = m;
@@ -1495,37 +1604,53 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
 
     fp->k = cfg.k;
     fp->wide = cfg.consumer_warps() == 8;
-    // Planar wall: every SPAD's frame coordinate along the voxel-line axis is the same
-    // float (the table below computes the same value per SPAD).
-    bool planar = cfg.k == 8;
-    {
-        const double *uk = u[cfg.kaxis];
-        float first = 0.0f;
-        for (uint64_t s = 0; s < fz.S && planar; s++) {
-            const float *pt = h_pairs[s].camera_point;
-            double d[3];
-            for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
-            const float gk = (float)(uk[0] * d[0] + uk[1] * d[1] + uk[2] * d[2]);
-            if (s == 0) first = gk;
-            planar = std::memcmp(&gk, &first, sizeof(float)) == 0;
-        }
+    // Device tables: SPAD entries (frame position relative to zero, row constant) and
+    // laser entries (frame position, lw/dT - t0/dT), built in FP64 on the GPU from the
+    // plan's device pair list (tables_fp64_kernel), which also tests the planar wall:
+    // every SPAD's FP32 frame coordinate along the voxel-line axis is the same float.
+    // d_diag: [0] timed-out waits, [1] window violations (read by fast_plan_check),
+    // [2..4] the table kernel's order / non-finite / off-plane counts.
+    const size_t tab_bytes = (fz.S + a.L) * sizeof(float4);
+    cudaError_t e = cudaMalloc(&fp->d_tables, tab_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, kPlanDiagWords * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(fp->d_diag, 0, kPlanDiagWords * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        fast_plan_free(fp);
+        return e == cudaErrorMemoryAllocation ? set_error(BPGB_ERR_OUT_OF_MEMORY, "fast plan tables")
+                                              : cuda_error(e, "fast plan tables");
     }
+    if (int ts = launch_tables(d_pairs, vol, u, (double)bp.dT, (double)bp.t0, a.L, fz.S, confocal,
+                               cfg.kaxis, fp->d_tables, fp->d_diag + 2, sm_count, 0)) {
+        fast_plan_free(fp);
+        return ts;
+    }
+    unsigned long long tdiag[3] = {0, 0, 0};
+    e = cudaMemcpy(tdiag, fp->d_diag + 2, sizeof(tdiag), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        fast_plan_free(fp);
+        return cuda_error(e, "fast plan table checks");
+    }
+    if (tdiag[0] || tdiag[1]) {  // the host factorisation and finiteness checks passed
+        fast_plan_free(fp);
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "device pair list disagrees with the host list");
+    }
+    const bool planar = cfg.k == 8 && tdiag[2] == 0;
     a.planar = planar && !fact ? 1 : 0;
     fp->planar = a.planar != 0;
     fp->fact = fact;
     void *kern = plan_kernel(fp);
     if (!kern) {
-        delete fp;
+        fast_plan_free(fp);
         return no("tile preset not built for this row type / accumulation");
     }
     if (int rs = reserve_dynamic_smem(kern, fp->smem)) {
-        delete fp;
+        fast_plan_free(fp);
         return rs;
     }
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)fp->threads, fp->smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)fp->threads, fp->smem);
     if (e != cudaSuccess || occ < 1) {
-        delete fp;
+        fast_plan_free(fp);
         return e != cudaSuccess ? cuda_error(e, "occupancy query")
                                 : no("fast kernel does not fit on an SM");
     }
@@ -1539,58 +1664,26 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d
     }
     splits = std::max<uint64_t>(1, std::min<uint64_t>(splits, items));
     if (ntiles * splits >= (1ull << 31)) {
-        delete fp;
+        fast_plan_free(fp);
         return no("grid too large");
     }
     a.splits = (uint32_t)splits;
     fp->grid = (uint32_t)(ntiles * splits);
     fp->a = a;
 
-    // Device tables: SPAD entries (frame position relative to zero, row constant) and
-    // laser entries (frame position, lw/dT - t0/dT), built in double on the host.
-    const double dT = bp.dT;
-    std::vector<float4> tab(fz.S + a.L);
-    auto frame = [&](const float *pt, double o[3]) {
-        double d[3];
-        for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
-        for (int r = 0; r < 3; r++) o[r] = u[r][0] * d[0] + u[r][1] * d[1] + u[r][2] * d[2];
-    };
-    for (uint64_t s = 0; s < fz.S; s++) {
-        const bpgb_pair &pr = h_pairs[s];
-        double f[3];
-        frame(pr.camera_point, f);
-        const double cs = confocal ? ((double)pr.camera_wall + (double)pr.laser_wall) / dT
-                                   : (double)pr.camera_wall / dT;
-        tab[s] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)cs);
-    }
-    for (uint64_t l = 0; l < a.L; l++) {
-        double f[3] = {0.0, 0.0, 0.0};
-        double c = -(double)bp.t0 / dT;
-        if (!confocal) {
-            const bpgb_pair &pr = h_pairs[l * fz.S];
-            frame(pr.laser_point, f);
-            c += (double)pr.laser_wall / dT;
-        }
-        tab[fz.S + l] = make_float4((float)f[0], (float)f[1], (float)f[2], (float)c);
-    }
-    const size_t tab_bytes = tab.size() * sizeof(float4);
     // partial sums: [split][voxel] for full launches, [slot][split][tile voxel] for
     // tile-list launches (tiles x tile voxels >= voxels)
     const size_t part_bytes =
         splits > 1 ? (size_t)splits * ntiles * a.tdim[0] * a.tdim[1] * a.tdim[2] *
                          (dt == BPGB_DTYPE_C64 || dt == BPGB_DTYPE_C32 ? 8 : 4)
                    : 0;
-    e = cudaMalloc(&fp->d_tables, tab_bytes);
-    if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess && part_bytes) e = cudaMalloc(&fp->d_partial, part_bytes);
-    if (e == cudaSuccess) e = cudaMemcpy(fp->d_tables, tab.data(), tab_bytes, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(fp->d_diag, 0, 2 * sizeof(unsigned long long));
+    if (part_bytes) e = cudaMalloc(&fp->d_partial, part_bytes);
     if (e != cudaSuccess) {
         fast_plan_free(fp);
         return e == cudaErrorMemoryAllocation ? set_error(BPGB_ERR_OUT_OF_MEMORY, "fast plan scratch")
-                                              : cuda_error(e, "fast plan tables");
+                                              : cuda_error(e, "fast plan scratch");
     }
-    fp->scratch = tab_bytes + part_bytes + 16;
+    fp->scratch = tab_bytes + part_bytes + kPlanDiagWords * sizeof(unsigned long long);
     *out = fp;
     return BPGB_OK;
 }
@@ -1605,8 +1698,9 @@ int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t s
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
     void *kern = plan_kernel(fp);
+    unsigned long long *diag = fp->d_diag;
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
-                    (void *)&fp->d_diag, (void *)&fp->a};
+                    (void *)&diag, (void *)&fp->a};
     BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(fp->grid), dim3(fp->threads), args, fp->smem, stream));
     count_launches(1);
     if (a.splits > 1) {
@@ -1762,6 +1856,15 @@ void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info) {
     info->smem_bytes = fp->smem;
     info->scratch_bytes = fp->scratch;
     info->factored = fp->fact ? 1 : 0;
+}
+
+int fast_plan_tables(const FastPlan *fp, float *host_out, uint64_t capacity, uint64_t *count) {
+    const uint64_t n = fp->a.S + fp->a.L;
+    if (count) *count = n;
+    const uint64_t m = std::min(n, capacity);
+    if (m && host_out)
+        BPGB_CUDA_TRY(cudaMemcpy(host_out, fp->d_tables, m * sizeof(float4), cudaMemcpyDeviceToHost));
+    return BPGB_OK;
 }
 
 int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts) {
@@ -2030,9 +2133,16 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     b->checked = o.checked != 0;
     if (o.spin_limit) b->spin_limit = o.spin_limit;
     std::vector<BatchCap> hc(n);
-    std::vector<float4> tabs;
+    struct TableJob {
+        uint32_t c;
+        Volume vol;
+        double u[3][3];
+        uint64_t L, S;
+        bool confocal;
+    };
+    std::vector<TableJob> tjobs;
+    uint64_t tab_count = 0;
     uint32_t max_row_bytes = 0, tmax = 0;
-    bool planar = true;
     for (uint32_t c = 0; c < n; c++) {
         const bpgb_capture_geometry &g = caps[c];
         auto fail = [&](int code, const std::string &m) {
@@ -2071,36 +2181,12 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
         a.spin_limit = b->spin_limit;
         max_row_bytes = std::max(max_row_bytes, a.row_bytes);
         tmax = std::max(tmax, g.T);
-        // tables (same FP64 arithmetic as a plan) and the planar-wall test
-        const double dT = g.deltaT;
-        auto frame = [&](const float *pt, double f[3]) {
-            double d[3];
-            for (int k = 0; k < 3; k++) d[k] = (double)pt[k] - (double)vol.zero[k];
-            for (int r = 0; r < 3; r++) f[r] = u[r][0] * d[0] + u[r][1] * d[1] + u[r][2] * d[2];
-        };
-        hc[c].tab_off = tabs.size();
-        float first = 0.0f;
-        for (uint64_t s = 0; s < fz.S; s++) {
-            const bpgb_pair &pr = g.pairs[s];
-            double f[3];
-            frame(pr.camera_point, f);
-            const double cs = confocal ? ((double)pr.camera_wall + (double)pr.laser_wall) / dT
-                                       : (double)pr.camera_wall / dT;
-            tabs.push_back(make_float4((float)f[0], (float)f[1], (float)f[2], (float)cs));
-            const float gk = (float)f[cfg.kaxis];
-            if (s == 0) first = gk;
-            planar = planar && std::memcmp(&gk, &first, sizeof(float)) == 0;
-        }
-        for (uint64_t l = 0; l < L; l++) {
-            double f[3] = {0.0, 0.0, 0.0};
-            double cst = -(double)g.t0 / dT;
-            if (!confocal) {
-                const bpgb_pair &pr = g.pairs[l * fz.S];
-                frame(pr.laser_point, f);
-                cst += (double)pr.laser_wall / dT;
-            }
-            tabs.push_back(make_float4((float)f[0], (float)f[1], (float)f[2], (float)cst));
-        }
+        // tables: built on the GPU after the loop (same FP64 kernel as a plan)
+        hc[c].tab_off = tab_count;
+        tab_count += fz.S + L;
+        tjobs.push_back({c, vol, {{u[0][0], u[0][1], u[0][2]}, {u[1][0], u[1][1], u[1][2]},
+                                  {u[2][0], u[2][1], u[2][2]}},
+                         L, fz.S, confocal});
         hc[c].row_base = b->total_rows;
         hc[c].out_off = b->total_vox;
         b->row_off.push_back(b->total_rows);
@@ -2112,6 +2198,41 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     if (b->total_rows >= (1ull << 31)) {
         batch_free(b);
         return set_error(BPGB_ERR_UNSUPPORTED, "batch has too many rows for TMA coordinates");
+    }
+    // Tables of every capture on the GPU in FP64 (tables_fp64_kernel, as for a plan) from
+    // the captures' pairs staged in one temporary device buffer, and the planar-wall
+    // test over all of them (each capture's SPADs against its own first SPAD).
+    bool planar = true;
+    {
+        bpgb_pair *d_pairs = nullptr;
+        cudaError_t e = cudaMalloc(&b->d_tables, tab_count * sizeof(float4));
+        if (e == cudaSuccess) e = cudaMalloc(&b->d_diag, kPlanDiagWords * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemset(b->d_diag, 0, kPlanDiagWords * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&d_pairs, b->total_rows * sizeof(bpgb_pair));
+        for (uint32_t c = 0; c < n && e == cudaSuccess; c++)
+            e = cudaMemcpy(d_pairs + b->row_off[c], caps[c].pairs,
+                           caps[c].num_pairs * sizeof(bpgb_pair), cudaMemcpyHostToDevice);
+        int ts = e == cudaSuccess ? BPGB_OK : cuda_error(e, "batch table inputs");
+        for (const TableJob &j : tjobs) {
+            if (ts) break;
+            const BinParams bp{caps[j.c].t0, caps[j.c].deltaT, caps[j.c].T};
+            ts = launch_tables(d_pairs + b->row_off[j.c], j.vol, j.u, (double)bp.dT, (double)bp.t0,
+                               j.L, j.S, j.confocal, cfg.kaxis, b->d_tables + hc[j.c].tab_off,
+                               b->d_diag + 2, sms, 0);
+        }
+        unsigned long long tdiag[3] = {0, 0, 0};
+        if (!ts) {
+            e = cudaMemcpy(tdiag, b->d_diag + 2, sizeof(tdiag), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) ts = cuda_error(e, "batch table checks");
+        }
+        if (d_pairs) cudaFree(d_pairs);
+        if (!ts && (tdiag[0] || tdiag[1]))
+            ts = set_error(BPGB_ERR_INVALID_ARGUMENT, "device pair lists disagree with the host lists");
+        if (ts) {
+            batch_free(b);
+            return ts;
+        }
+        planar = tdiag[2] == 0;
     }
     // One stage ring per launch: the widest window among that launch's captures sets its
     // row slot.  The per-pair launch targets three CTAs per SM (72 KB of shared memory
@@ -2249,14 +2370,9 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     if (scratch) e = cudaMalloc(&b->d_scratch, scratch * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_caps, n * sizeof(BatchCap));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_units, sorted.size() * sizeof(BatchUnit));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4));
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_diag, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemcpy(b->d_caps, hc.data(), n * sizeof(BatchCap), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_units, sorted.data(), sorted.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(b->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(b->d_diag, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(b->d_sched, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
@@ -2377,83 +2493,6 @@ constexpr size_t kNoAllocDiagBytes = 256;  // counters; the tables start 256 B i
 // cudaGetSymbolAddress (noalloc_scratch_ptr below).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-struct NoAllocTableArgs {
-    double u[3][3];
-    double zero[3];
-    double dT, t0;
-    uint64_t L, S;
-    int confocal;
-    uint32_t kax;  // voxel-line axis of the tile preset (planar-wall test)
-};
-
-__device__ __forceinline__ void frame_fp64(const NoAllocTableArgs &t, const float *pt, double o[3]) {
-    const double d0 = __dsub_rn((double)pt[0], t.zero[0]);
-    const double d1 = __dsub_rn((double)pt[1], t.zero[1]);
-    const double d2 = __dsub_rn((double)pt[2], t.zero[2]);
-    for (int r = 0; r < 3; r++)
-        o[r] = __dadd_rn(__dadd_rn(__dmul_rn(t.u[r][0], d0), __dmul_rn(t.u[r][1], d1)),
-                         __dmul_rn(t.u[r][2], d2));
-}
-
-__device__ __forceinline__ bool same_point(const float *a, const float *b) {
-    return __float_as_uint(a[0]) == __float_as_uint(b[0]) &&
-           __float_as_uint(a[1]) == __float_as_uint(b[1]) &&
-           __float_as_uint(a[2]) == __float_as_uint(b[2]);
-}
-
-// Tables of the FAST kernel from a device pair list (same FP64 arithmetic as the plan's
-// host build), plus a check that the list has the stated order p = l * S + s (or is
-// confocal): diag[2] counts pairs that break it, diag[3] non-finite values.
-__global__ void noalloc_tables_kernel(const bpgb_pair *__restrict__ pairs, const NoAllocTableArgs t,
-                                      float4 *__restrict__ tab, unsigned long long *__restrict__ diag) {
-    const uint64_t P = t.L * t.S;
-    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P;
-         p += (uint64_t)gridDim.x * blockDim.x) {
-        const bpgb_pair pr = pairs[p];
-        const uint64_t l = p / t.S, s = p % t.S;
-        const float *f = reinterpret_cast<const float *>(&pr);
-        bool finite = true;
-        for (int k = 0; k < 8; k++) finite = finite && isfinite(f[k]);
-        if (!finite) atomicAdd(&diag[3], 1ull);
-        bool ok;
-        if (t.confocal) {
-            ok = same_point(pr.laser_point, pr.camera_point) &&
-                 __float_as_uint(pr.laser_wall) == __float_as_uint(pr.camera_wall);
-        } else {
-            const bpgb_pair &head = pairs[l * t.S];
-            const bpgb_pair &col = pairs[s];
-            ok = same_point(pr.laser_point, head.laser_point) &&
-                 __float_as_uint(pr.laser_wall) == __float_as_uint(head.laser_wall) &&
-                 same_point(pr.camera_point, col.camera_point) &&
-                 __float_as_uint(pr.camera_wall) == __float_as_uint(col.camera_wall);
-        }
-        if (!ok) atomicAdd(&diag[2], 1ull);
-        if (l == 0) {
-            double g[3];
-            frame_fp64(t, pr.camera_point, g);
-            const double cs = t.confocal
-                                  ? __ddiv_rn(__dadd_rn((double)pr.camera_wall, (double)pr.laser_wall), t.dT)
-                                  : __ddiv_rn((double)pr.camera_wall, t.dT);
-            tab[s] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)cs);
-            // planar wall: the same FP32 frame coordinate along kax as SPAD 0 (diag[4]
-            // counts SPADs off that plane)
-            double g0[3];
-            frame_fp64(t, pairs[0].camera_point, g0);
-            if (__float_as_uint((float)g[t.kax]) != __float_as_uint((float)g0[t.kax]))
-                atomicAdd(&diag[4], 1ull);
-        }
-        if (s == 0) {
-            double g[3] = {0.0, 0.0, 0.0};
-            double c = __ddiv_rn(-t.t0, t.dT);
-            if (!t.confocal) {
-                frame_fp64(t, pr.laser_point, g);
-                c = __dadd_rn(c, __ddiv_rn((double)pr.laser_wall, t.dT));
-            }
-            tab[t.S + l] = make_float4((float)g[0], (float)g[1], (float)g[2], (float)c);
-        }
-    }
-}
-
 // Device address of g_noalloc_scratch, resolved once per device with that device
 // current (the symbol's host-side name is only a stand-in, never a device pointer).
 int noalloc_scratch_ptr(unsigned char **out) {
@@ -2536,9 +2575,37 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     st = fast_args(a, cfg, vol, hd, confocal != 0, deltaT, t0, num_lasers, num_spads, T, 4, false,
                    0, 0, &why);
     if (st) return set_error(st, why);
+
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long *diag = reinterpret_cast<unsigned long long *>(scratch);
+    float4 *tab = reinterpret_cast<float4 *>(scratch + kNoAllocDiagBytes);
+    // The array keeps the previous call's contents: the counters must start at zero.
+    BPGB_CUDA_TRY(cudaMemsetAsync(diag, 0, kNoAllocDiagBytes, s));
+    // Tables in FP64 from the caller's device pair list (the kernel a plan uses); its
+    // checks land in diag[2..4]: pairs out of the stated order, non-finite values, SPADs
+    // off the planar wall.
+    st = launch_tables(d_pairs, vol, u, (double)deltaT, (double)t0, num_lasers, num_spads,
+                       confocal != 0, cfg.kaxis, tab, diag + 2, sms, s);
+    if (st) return st;
+    // A pair list with non-finite values or another order never reaches the window
+    // arithmetic of the main kernel.
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    BPGB_CUDA_TRY(cudaMemcpyAsync(h, diag, sizeof(h), cudaMemcpyDeviceToHost, s));
+    BPGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[3]) return set_error(BPGB_ERR_INVALID_ARGUMENT, std::to_string(h[3]) + " non-finite pair values");
+    if (h[2])
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         std::to_string(h[2]) + " pairs break the stated lasers x SPADs order");
+
+    // The kernel variant a plan on these pairs runs (the planar-wall form when every SPAD
+    // lies on one plane across the voxel lines; the 8-warp build when the preset has 8
+    // consumer warps), selected before its occupancy sets the pair splits, as in a plan.
+    a.planar = (h[4] == 0 && cfg.k == 8) ? 1 : 0;
     const uint32_t threads = fast_threads(cfg);
     const uint32_t smem = fast_smem(a);
-    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, false, true);  // general form first
+    void *kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, a.planar != 0,
+                               cfg.consumer_warps() == 8);
+    if (!kern) return set_error(BPGB_ERR_UNSUPPORTED, "default tile preset not built for FP32 rows");
     st = reserve_dynamic_smem(kern, smem);
     if (st) return st;
     int occ = 0;
@@ -2556,44 +2623,7 @@ extern "C" int bpgb_backproject_noalloc(const float *d_H, uint32_t T, uint32_t h
     splits = std::max<uint64_t>(1, std::min<uint64_t>({splits, items, max_splits}));
     if (ntiles * splits >= (1ull << 31)) return set_error(BPGB_ERR_UNSUPPORTED, "grid too large");
     a.splits = (uint32_t)splits;
-
-    cudaStream_t s = (cudaStream_t)stream;
-    unsigned long long *diag = reinterpret_cast<unsigned long long *>(scratch);
-    float4 *tab = reinterpret_cast<float4 *>(scratch + kNoAllocDiagBytes);
     float *partial = reinterpret_cast<float *>(scratch + part_off);
-    // The array keeps the previous call's contents: the counters must start at zero.
-    BPGB_CUDA_TRY(cudaMemsetAsync(diag, 0, kNoAllocDiagBytes, s));
-    NoAllocTableArgs ta{};
-    for (int r = 0; r < 3; r++)
-        for (int k = 0; k < 3; k++) ta.u[r][k] = u[r][k];
-    for (int k = 0; k < 3; k++) ta.zero[k] = (double)vol.zero[k];
-    ta.dT = (double)deltaT;
-    ta.t0 = (double)t0;
-    ta.L = num_lasers;
-    ta.S = num_spads;
-    ta.confocal = confocal ? 1 : 0;
-    ta.kax = cfg.kaxis;
-    const unsigned tblocks = (unsigned)std::min<uint64_t>((P + 255) / 256, 152ull * 16);
-    noalloc_tables_kernel<<<tblocks, 256, 0, s>>>(d_pairs, ta, tab, diag);
-    count_launches(1);
-    BPGB_CUDA_TRY(cudaGetLastError());
-    // A pair list with non-finite values or another order never reaches the window
-    // arithmetic of the main kernel.
-    unsigned long long h[5] = {0, 0, 0, 0, 0};
-    BPGB_CUDA_TRY(cudaMemcpyAsync(h, diag, sizeof(h), cudaMemcpyDeviceToHost, s));
-    BPGB_CUDA_TRY(cudaStreamSynchronize(s));
-    if (h[3]) return set_error(BPGB_ERR_INVALID_ARGUMENT, std::to_string(h[3]) + " non-finite pair values");
-    if (h[2])
-        return set_error(BPGB_ERR_INVALID_ARGUMENT,
-                         std::to_string(h[2]) + " pairs break the stated lasers x SPADs order");
-    // Same kernel variant as a plan on these pairs: the planar-wall form when every SPAD
-    // lies on one plane across the voxel lines.
-    if (h[4] == 0 && cfg.k == 8) {
-        a.planar = 1;
-        kern = select_kernel(BPGB_DTYPE_F32, false, false, cfg.k, true, true);
-        st = reserve_dynamic_smem(kern, smem);
-        if (st) return st;
-    }
 
     CUtensorMap map;
     st = encode_rows(&map, BPGB_DTYPE_F32, d_H, T, P, pitch, a.BW);

@@ -93,10 +93,11 @@ FastConfig fast_preset(int index, int dtype);
 int fast_preset_count();
 
 struct FastPlan;  // opaque, defined in bp_fast.cu
-int fast_plan_build(FastPlan **out, const bpgb_pair *h_pairs, const bpgb_pair *d_pairs,
-                    uint64_t P, const Factorization &fz, const Volume &vol,
-                    const BinParams &bp, const bpgb_options &opt, int sm_count,
-                    std::string *why_not);
+// Tables are built on the GPU in FP64 from the plan's device pair list d_pairs (the
+// host list was already factorised into fz).
+int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
+                    const Factorization &fz, const Volume &vol, const BinParams &bp,
+                    const bpgb_options &opt, int sm_count, std::string *why_not);
 int fast_plan_execute(FastPlan *fp, const void *d_H, void *d_out, cudaStream_t stream);
 int fast_plan_dump_bins(FastPlan *fp, const int64_t *d_ids, int64_t n, int32_t *d_bins,
                         cudaStream_t stream);
@@ -106,6 +107,7 @@ int fast_plan_select_tiles(FastPlan *fp, const float *d_score, const uint32_t *b
                            uint32_t block_size, float threshold, uint32_t *d_list,
                            uint32_t *d_count, cudaStream_t stream);
 void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info);
+int fast_plan_tables(const FastPlan *fp, float *host_out, uint64_t capacity, uint64_t *count);
 int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts);
 void fast_plan_free(FastPlan *fp);
 int wait_timeout_probe(uint32_t limit, int *timed_out);

@@ -340,7 +340,7 @@ int bpgb_plan_create(bpgb_plan *plan, const bpgb_pair *host_pairs, uint64_t num_
                              "EXACT computes FP32/complex64 rows with FP32 sums only");
         }
         why.clear();
-        st = num_pairs ? fast_plan_build(&p->fast, host_pairs, p->d_pairs, num_pairs, p->fz,
+        st = num_pairs ? fast_plan_build(&p->fast, p->d_pairs, num_pairs, p->fz,
                                          p->vol, p->bp, o, sms, &why)
                        : BPGB_ERR_UNSUPPORTED;
         if (st == BPGB_OK) {
@@ -473,6 +473,15 @@ int bpgb_plan_dump_bins(bpgb_plan plan, const int64_t *h_voxel_ids, int64_t n, i
     if (st) return st;
     if (e != cudaSuccess) return cuda_error(e, "dump bins");
     return BPGB_OK;
+}
+
+int bpgb_plan_get_tables(bpgb_plan plan, float *host_out, uint64_t capacity,
+                         uint64_t *num_entries) {
+    clear_error();
+    if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");
+    if (plan->algo != BPGB_ALGO_FAST || !plan->fast)
+        return set_error(BPGB_ERR_UNSUPPORTED, "tables belong to FAST plans");
+    return fast_plan_tables(plan->fast, host_out, capacity, num_entries);
 }
 
 int bpgb_plan_destroy(bpgb_plan plan) {

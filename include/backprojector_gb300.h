@@ -193,6 +193,16 @@ int bpgb_plan_get_info(bpgb_plan plan, bpgb_plan_info *info);
  * d_bins[i * P + p] (int32, -1 = outside [0, T)).  For parity measurement only. */
 int bpgb_plan_dump_bins(bpgb_plan plan, const int64_t *h_voxel_ids, int64_t n,
                         int32_t *d_bins, void *stream);
+/* The FAST plan's FP32 tables, built on the GPU in FP64 from the pair list (the values
+ * precompute_distances keeps in double, backproject.hpp:356-418, plus the volume frame):
+ * num_spads SPAD entries {x, y, z, camera_wall / deltaT} ((camera_wall + laser_wall) /
+ * deltaT when confocal), then num_lasers laser entries {x, y, z, laser_wall / deltaT -
+ * t0 / deltaT}, positions in the voxel basis' orthonormal frame relative to
+ * volume_zero_pos (metres).  Copies min(capacity, count) entries of 4 floats to host_out
+ * and the count to *num_entries.  For inspection and tests; BPGB_ERR_UNSUPPORTED for
+ * EXACT plans. */
+int bpgb_plan_get_tables(bpgb_plan plan, float *host_out, uint64_t capacity,
+                         uint64_t *num_entries);
 int bpgb_plan_destroy(bpgb_plan plan);
 
 /* ---- allocation-free backprojection ----------------------------------------

@@ -68,6 +68,27 @@ def test_noalloc_matches_plan_path_twice(cuda, name, kw, L):
         assert oracle.rel_l2(got, ref) < 5e-3
 
 
+def test_noalloc_large_volume_direct_store(cuda):
+    """A 256^3 volume (67 MB of FP32) leaves no room for per-split partial sums in the
+    16 MiB array: the call runs unsplit and stores straight into the volume.  Checked
+    against the FP64 oracle on seeded voxels and against a plan, whose own split count
+    may differ (sums in another order, hence 1e-5)."""
+    import torch
+
+    cap = synthetic.make_capture("octree_256", seed=31, spad_grid=(16, 16))
+    dH = torch.from_numpy(cap.H).to(cuda)
+    dP = torch.from_numpy(cap.pairs.view(np.uint8).copy()).to(cuda)
+    dV = torch.full(tuple(int(v) for v in cap.voxels_per_side), float("nan"), device=cuda)
+    for _ in range(2):
+        got = noalloc(cap, dH, dP, dV, 1, cap.P)
+        assert np.isfinite(got).all()
+        assert oracle.rel_l2(got, plan_result(cap, dH)) < 1e-5
+    ids = np.random.default_rng(3).choice(cap.nvox, 2048, replace=False)
+    ref = oracle.bp_gpu_f64(cap.H, cap.pairs, cap.voxels_per_side, cap.zero, cap.inc, cap.t0,
+                            cap.deltaT, voxels=ids)
+    assert oracle.rel_l2(got.reshape(-1)[ids], ref) < 5e-3
+
+
 def test_noalloc_rejects_bad_requests(cuda):
     import torch
 
