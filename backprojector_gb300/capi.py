@@ -126,6 +126,8 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "bpgb_plan_get_info": (C.c_int, [_P, C.POINTER(PlanInfo)]),
     "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
+    "bpgb_set_dropin_algo": (C.c_int, [C.c_int]),
+    "bpgb_get_dropin_algo": (C.c_int, []),
     "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     "bpgb_plan_destroy": (C.c_int, [_P]),
     "bpgb_diag_wait_timeout": (C.c_int, [C.c_uint32]),

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -576,6 +577,40 @@ int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, 
     return st;
 }
 
+}  // extern "C"
+
+namespace {
+// Algorithm of the drop-in calls (bpgb_backproject_f32 / _c64 and the call_cuda_* shim):
+// BPGB_ALGO=exact|fast|auto in the environment at first use, bpgb_set_dropin_algo after.
+std::atomic<int> g_dropin_algo{-1};
+
+int dropin_algo() {
+    int a = g_dropin_algo.load(std::memory_order_relaxed);
+    if (a >= 0) return a;
+    a = BPGB_ALGO_AUTO;
+    if (const char *e = std::getenv("BPGB_ALGO")) {
+        const std::string v(e);
+        if (v == "exact" || v == "EXACT" || v == "1") a = BPGB_ALGO_EXACT;
+        else if (v == "fast" || v == "FAST" || v == "2") a = BPGB_ALGO_FAST;
+    }
+    int expected = -1;
+    g_dropin_algo.compare_exchange_strong(expected, a);
+    return g_dropin_algo.load(std::memory_order_relaxed);
+}
+}  // namespace
+
+extern "C" {
+
+int bpgb_set_dropin_algo(int algo) {
+    clear_error();
+    if (algo != BPGB_ALGO_AUTO && algo != BPGB_ALGO_EXACT && algo != BPGB_ALGO_FAST)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "algo must be BPGB_ALGO_AUTO, _EXACT or _FAST");
+    g_dropin_algo.store(algo, std::memory_order_relaxed);
+    return BPGB_OK;
+}
+
+int bpgb_get_dropin_algo(void) { return dropin_algo(); }
+
 int bpgb_backproject_f32(const float *transient_chunk, uint64_t transient_size, uint32_t T,
                          const bpgb_pair *scanned_pairs, uint64_t num_pairs,
                          float *voxel_volume, const uint32_t *voxels_per_side,
@@ -583,6 +618,7 @@ int bpgb_backproject_f32(const float *transient_chunk, uint64_t transient_size, 
                          float deltaT) {
     bpgb_options o;
     bpgb_options_default(&o);
+    o.algo = dropin_algo();
     o.h_dtype = BPGB_DTYPE_F32;
     return bpgb_backproject_host(transient_chunk, transient_size, T, scanned_pairs, num_pairs,
                                  voxel_volume, voxels_per_side, volume_zero_pos, voxel_inc, t0,
@@ -596,6 +632,7 @@ int bpgb_backproject_c64(const float *transient_chunk, uint64_t transient_size, 
                          float deltaT) {
     bpgb_options o;
     bpgb_options_default(&o);
+    o.algo = dropin_algo();
     o.h_dtype = BPGB_DTYPE_C64;
     return bpgb_backproject_host(transient_chunk, transient_size, T, scanned_pairs, num_pairs,
                                  voxel_volume, voxels_per_side, volume_zero_pos, voxel_inc, t0,

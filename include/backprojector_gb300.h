@@ -135,7 +135,8 @@ uint64_t bpgb_launch_count(void);
  * every pair is used (it skips the last P mod blockDim pairs) and every voxel is
  * visited exactly once for any N (its voxel cursor wraps and recomputes some voxels
  * when N is not a multiple of 16, backproject_cuda.cu:65-80).
- * ALGO_AUTO, FP32 accumulation.  Replaces backproject_cuda.cu:370-500 / 671-801. */
+ * Algorithm as set by bpgb_set_dropin_algo / BPGB_ALGO (below; default ALGO_AUTO), FP32
+ * accumulation.  Replaces backproject_cuda.cu:370-500 / 671-801. */
 int bpgb_backproject_f32(const float *transient_chunk, uint64_t transient_size, uint32_t T,
                          const bpgb_pair *scanned_pairs, uint64_t num_pairs,
                          float *voxel_volume, const uint32_t *voxels_per_side,
@@ -147,6 +148,13 @@ int bpgb_backproject_c64(const float *transient_chunk, uint64_t transient_size, 
                          float *voxel_volume, const uint32_t *voxels_per_side,
                          const float *volume_zero_pos, const float *voxel_inc, float t0,
                          float deltaT);
+/* Algorithm of bpgb_backproject_f32 / _c64 (and so of the call_cuda_* C++ drop-in):
+ * BPGB_ALGO_AUTO (default: FAST where the pair list factors, else EXACT), BPGB_ALGO_EXACT
+ * (the reference kernel's FP32 expression: bins bit-identical to call_cuda_backprojection)
+ * or BPGB_ALGO_FAST.  The environment variable BPGB_ALGO=exact|fast|auto sets the initial
+ * value, read at the first drop-in call; bpgb_set_dropin_algo overrides it process-wide. */
+int bpgb_set_dropin_algo(int algo);
+int bpgb_get_dropin_algo(void);
 /* As bpgb_backproject_f32/_c64 with explicit options (algo, accumulation). */
 int bpgb_backproject_host(const void *transient_chunk, uint64_t transient_size, uint32_t T,
                           const bpgb_pair *scanned_pairs, uint64_t num_pairs,

@@ -3,8 +3,8 @@ checked per capture against single-capture plans and the FP64 oracle.
 
 Tolerances: against a plan on the same stored rows the batch has the same bins and
 summation order (rel-L2 <= 1e-6).  FP16 rows dequantised with the per-capture scale feed
-the FP64 oracle, so the batch differs from it by FAST binning only: rel-L2 <= 5e-3 on
-captures of >= 256 pairs (as for plans) and <= 2e-2 on the 16-64-pair captures of these
+the FP64 oracle, so the batch differs from it by FAST binning only: rel-L2 <= 1e-3 on
+captures of >= 1024 pairs (as for plans) and <= 2e-2 on the 16-256-pair captures of these
 small batches, where one bin placed one bin over moves a voxel by about 1/P of its sum.
 """
 from __future__ import annotations
@@ -29,7 +29,7 @@ def tol(c):
     # captures: one flipped bin moves a voxel by ~1/P of its sum.  Measured on the 256-pair
     # lasers x SPADs captures: mis-binned fraction 2-4e-5 for both the factored and the
     # per-pair form, rel-L2 up to 1.06e-2.
-    return 5e-3 if c.P >= 1024 else 2e-2
+    return 1e-3 if c.P >= 1024 else 2e-2
 
 
 def upload(cuda, caps, batch, dtype, scales):
