@@ -126,6 +126,11 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_check": (C.c_int, [_P, C.POINTER(C.c_uint64)]),
     "bpgb_plan_get_info": (C.c_int, [_P, C.POINTER(PlanInfo)]),
     "bpgb_plan_dump_bins": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64, _P, _P]),
+    "bpgb_eval_f64_voxels": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, _P, C.c_uint64, _P,
+                                       _P, _P, C.c_float, C.c_float, _P, C.c_int64, _P, _P]),
+    "bpgb_block_detail": (C.c_int, [_P, _U32, _P, _U32, _U32, C.c_uint32, C.c_uint32, _P,
+                                    C.c_float, _P, _P]),
+    "bpgb_plan_select_tiles_topk": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "bpgb_set_dropin_algo": (C.c_int, [C.c_int]),
     "bpgb_get_dropin_algo": (C.c_int, []),
     "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -440,6 +445,14 @@ class Plan:
                                            _ptr(d_tile_count), _stream_ptr(stream)),
               "bpgb_plan_select_tiles")
 
+    def select_tiles_topk(self, d_score, block_dims, block_size: int, k: int, d_tile_list,
+                          d_tile_count, stream=None) -> None:
+        check(lib().bpgb_plan_select_tiles_topk(self.handle, _ptr(d_score),
+                                                u32ptr(_dims(block_dims)), block_size, int(k),
+                                                _ptr(d_tile_list), _ptr(d_tile_count),
+                                                _stream_ptr(stream)),
+              "bpgb_plan_select_tiles_topk")
+
     def dump_bins(self, voxel_ids, d_bins, stream=None) -> None:
         ids = np.ascontiguousarray(np.asarray(voxel_ids, dtype=np.int64))
         check(lib().bpgb_plan_dump_bins(self.handle, ids.ctypes.data_as(C.POINTER(C.c_int64)),
@@ -471,6 +484,17 @@ class Plan:
 
     def __exit__(self, *a):
         self.close()
+
+
+def eval_f64_voxels(d_H, T: int, d_pairs, num_pairs: int, voxels_per_side, zero, inc,
+                    t0: float, deltaT: float, d_voxel_ids, d_out, h_pitch: int = 0,
+                    is_complex: bool = False, stream=None) -> None:
+    """FP64 values of the listed voxels (device int64 ids -> device float64 out)."""
+    check(lib().bpgb_eval_f64_voxels(_ptr(d_H), 1 if is_complex else 0, T, h_pitch, _ptr(d_pairs),
+                                     num_pairs, u32ptr(_dims(voxels_per_side)), fptr(f32(zero)),
+                                     fptr(f32(inc)), t0, deltaT, _ptr(d_voxel_ids),
+                                     int(d_voxel_ids.numel()), _ptr(d_out), _stream_ptr(stream)),
+          "bpgb_eval_f64_voxels")
 
 
 def phasor_pulse_device(d_H, rows: int, T: int, in_pitch: int, wavelength: float, deltaT: float,
@@ -629,6 +653,16 @@ def upsample_trilinear(d_coarse, coarse_dims, d_fine, fine_dims, stream=None) ->
     check(lib().bpgb_upsample_trilinear(_ptr(d_coarse), u32ptr(_dims(coarse_dims)), _ptr(d_fine),
                                         u32ptr(_dims(fine_dims)), _stream_ptr(stream)),
           "bpgb_upsample_trilinear")
+
+
+def block_detail(d_coarse_lo, lo_dims, d_coarse_hi, hi_dims, fine_dims, block_size: int,
+                 d_score, samples: int = 4, d_logits=None, logit_lo: float = 0.0,
+                 stream=None) -> None:
+    check(lib().bpgb_block_detail(_ptr(d_coarse_lo), u32ptr(_dims(lo_dims)), _ptr(d_coarse_hi),
+                                  u32ptr(_dims(hi_dims)), u32ptr(_dims(fine_dims)), block_size,
+                                  samples, _ptr(d_logits) if d_logits is not None else None,
+                                  logit_lo, _ptr(d_score), _stream_ptr(stream)),
+          "bpgb_block_detail")
 
 
 def cnn_kp(cin: int) -> int:

@@ -61,6 +61,7 @@ constexpr uint32_t kMaxChunk = 64;                         // rows per stage (tw
 constexpr uint32_t kFactS = 4;  // SPADs per block of the factored lasers x SPADs form
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
 constexpr uint32_t kPlanDiagWords = 8;  // a plan's device counters (see fast_plan_build)
+constexpr uint32_t kPlanThresholdWord = 5;  // ... and the top-k selection's threshold
 // row records of a chunk of c rows, padded so that the TMA rows after them stay aligned
 __host__ __device__ constexpr uint32_t table_bytes_of(uint32_t c) {
     return (c * kRecordBytes + 127) / 128 * 128;
@@ -1609,7 +1610,8 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
     // plan's device pair list (tables_fp64_kernel), which also tests the planar wall:
     // every SPAD's FP32 frame coordinate along the voxel-line axis is the same float.
     // d_diag: [0] timed-out waits, [1] window violations (read by fast_plan_check),
-    // [2..4] the table kernel's order / non-finite / off-plane counts.
+    // [2..4] the table kernel's order / non-finite / off-plane counts, [5] the top-k tile
+    // selection's score threshold.
     const size_t tab_bytes = (fz.S + a.L) * sizeof(float4);
     cudaError_t e = cudaMalloc(&fp->d_tables, tab_bytes);
     if (e == cudaSuccess) e = cudaMalloc(&fp->d_diag, kPlanDiagWords * sizeof(unsigned long long));
@@ -1780,14 +1782,17 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
 namespace {
 
 // One thread per tile of the plan (tile order of tile_of_block): the tile is listed when
-// any score block it overlaps is above the threshold.  Blocks are bs^3 voxels on the
+// any score block it overlaps is above the threshold (at or above it when `ge`; the
+// threshold read from device memory when d_thr is given).  Blocks are bs^3 voxels on the
 // plan's voxel grid; list order depends on thread timing, results of a tile-list launch
 // do not (every tile is computed on its own).
 __global__ void select_tiles_kernel(const float *__restrict__ score, uint32_t bnx, uint32_t bny,
-                                    uint32_t bnz, uint32_t bs, float threshold, uint32_t t0n,
+                                    uint32_t bnz, uint32_t bs, float threshold,
+                                    const float *__restrict__ d_thr, int ge, uint32_t t0n,
                                     uint32_t t1n, uint32_t t2n, uint32_t d0, uint32_t d1,
                                     uint32_t d2, uint32_t *__restrict__ list,
                                     uint32_t *__restrict__ count) {
+    const float thr = d_thr ? *d_thr : threshold;
     const uint32_t ntiles = t0n * t1n * t2n;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles;
          t += gridDim.x * blockDim.x) {
@@ -1799,10 +1804,51 @@ __global__ void select_tiles_kernel(const float *__restrict__ score, uint32_t bn
         bool any = false;
         for (uint32_t x = lo[0]; x <= hi[0] && !any; x++)
             for (uint32_t y = lo[1]; y <= hi[1] && !any; y++)
-                for (uint32_t z = lo[2]; z <= hi[2] && !any; z++)
-                    any = score[((uint64_t)x * bny + y) * bnz + z] > threshold;
+                for (uint32_t z = lo[2]; z <= hi[2] && !any; z++) {
+                    const float v = score[((uint64_t)x * bny + y) * bnz + z];
+                    any = ge ? v >= thr : v > thr;
+                }
         if (any) list[atomicAdd(count, 1u)] = t;
     }
+}
+
+// The k-th largest of n non-negative scores (NaN and negative values count as 0), by
+// radix selection on their float bits, which order like the values: four passes over
+// 8-bit digits, most significant first, each a shared-memory histogram of the scores
+// that share the digits chosen so far.  One CTA; writes the score to *out.
+__global__ void __launch_bounds__(1024) topk_threshold_kernel(const float *__restrict__ score,
+                                                              uint32_t n, uint32_t k,
+                                                              float *__restrict__ out) {
+    __shared__ uint32_t hist[256];
+    __shared__ uint32_t prefix, mask, rest;
+    if (threadIdx.x == 0) {
+        prefix = 0;
+        mask = 0;
+        rest = k;
+    }
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const uint32_t pf = prefix, mk = mask;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const float v = score[i];
+            const uint32_t key = v > 0.0f ? __float_as_uint(v) : 0u;
+            if ((key & mk) == pf) atomicAdd(&hist[(key >> shift) & 0xFFu], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t cum = 0, d = 255;
+            for (;; d--) {
+                if (cum + hist[d] >= rest || d == 0) break;
+                cum += hist[d];
+            }
+            rest -= cum;
+            prefix = pf | (d << shift);
+            mask = mk | (0xFFu << shift);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = __uint_as_float(prefix);
 }
 
 }  // namespace
@@ -1820,10 +1866,37 @@ int fast_plan_select_tiles(FastPlan *fp, const float *d_score, const uint32_t *b
     BPGB_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), stream));
     const unsigned blocks = (ntiles + 255) / 256;
     select_tiles_kernel<<<blocks, 256, 0, stream>>>(d_score, block_dims[0], block_dims[1],
-                                                    block_dims[2], block_size, threshold,
-                                                    a.tiles[0], a.tiles[1], a.tiles[2], a.tdim[0],
-                                                    a.tdim[1], a.tdim[2], d_list, d_count);
+                                                    block_dims[2], block_size, threshold, nullptr,
+                                                    0, a.tiles[0], a.tiles[1], a.tiles[2],
+                                                    a.tdim[0], a.tdim[1], a.tdim[2], d_list,
+                                                    d_count);
     count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+int fast_plan_select_tiles_topk(FastPlan *fp, const float *d_score, const uint32_t *block_dims,
+                                uint32_t block_size, uint32_t k, uint32_t *d_list,
+                                uint32_t *d_count, cudaStream_t stream) {
+    const FastArgs &a = fp->a;
+    if (!d_score || !block_dims || !d_list || !d_count || block_size == 0)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "null argument");
+    for (int q = 0; q < 3; q++)
+        if (block_dims[q] == 0 || (uint64_t)block_dims[q] * block_size < a.n[q])
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "score blocks do not cover the volume");
+    const uint64_t nb = (uint64_t)block_dims[0] * block_dims[1] * block_dims[2];
+    if (nb >= (1ull << 32)) return set_error(BPGB_ERR_UNSUPPORTED, "too many score blocks");
+    BPGB_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(uint32_t), stream));
+    if (k == 0) return BPGB_OK;
+    const uint32_t kk = (uint32_t)std::min<uint64_t>(k, nb);
+    // the threshold lives in the plan's device counters (word kPlanThresholdWord)
+    float *d_thr = reinterpret_cast<float *>(fp->d_diag + kPlanThresholdWord);
+    topk_threshold_kernel<<<1, 1024, 0, stream>>>(d_score, (uint32_t)nb, kk, d_thr);
+    const uint32_t ntiles = a.tiles[0] * a.tiles[1] * a.tiles[2];
+    select_tiles_kernel<<<(ntiles + 255) / 256, 256, 0, stream>>>(
+        d_score, block_dims[0], block_dims[1], block_dims[2], block_size, 0.0f, d_thr, 1,
+        a.tiles[0], a.tiles[1], a.tiles[2], a.tdim[0], a.tdim[1], a.tdim[2], d_list, d_count);
+    count_launches(2);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
 }

@@ -106,6 +106,9 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
 int fast_plan_select_tiles(FastPlan *fp, const float *d_score, const uint32_t *block_dims,
                            uint32_t block_size, float threshold, uint32_t *d_list,
                            uint32_t *d_count, cudaStream_t stream);
+int fast_plan_select_tiles_topk(FastPlan *fp, const float *d_score, const uint32_t *block_dims,
+                                uint32_t block_size, uint32_t k, uint32_t *d_list,
+                                uint32_t *d_count, cudaStream_t stream);
 void fast_plan_info(const FastPlan *fp, bpgb_plan_info *info);
 int fast_plan_tables(const FastPlan *fp, float *host_out, uint64_t capacity, uint64_t *count);
 int fast_plan_check(FastPlan *fp, uint64_t *violations, uint64_t *timeouts);

@@ -408,6 +408,17 @@ int bpgb_plan_select_tiles(bpgb_plan plan, const float *d_block_score,
                                   d_tile_list, d_tile_count, (cudaStream_t)stream);
 }
 
+int bpgb_plan_select_tiles_topk(bpgb_plan plan, const float *d_block_score,
+                                const uint32_t *block_dims, uint32_t block_size, uint32_t k,
+                                uint32_t *d_tile_list, uint32_t *d_tile_count, void *stream) {
+    clear_error();
+    if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");
+    if (plan->algo != BPGB_ALGO_FAST || !plan->fast)
+        return set_error(BPGB_ERR_UNSUPPORTED, "tile selection needs a FAST plan");
+    return fast_plan_select_tiles_topk(plan->fast, d_block_score, block_dims, block_size, k,
+                                       d_tile_list, d_tile_count, (cudaStream_t)stream);
+}
+
 int bpgb_plan_check(bpgb_plan plan, uint64_t *violations) {
     clear_error();
     if (!plan) return set_error(BPGB_ERR_INVALID_ARGUMENT, "plan is null");

@@ -159,6 +159,73 @@ __global__ void laplacian7_kernel(const float *__restrict__ vol, uint32_t n0, ui
     }
 }
 
+// Trilinear sample of a coarse grid spanning the fine grid's box at fine index
+// (x, y, z), with upsample_kernel's coordinate mapping and clamping.
+__device__ __forceinline__ float trilinear_at(const float *__restrict__ c, uint32_t c0,
+                                              uint32_t c1, uint32_t c2, float s0, float s1,
+                                              float s2, uint32_t x, uint32_t y, uint32_t z) {
+    const float u0 = x * s0, u1 = y * s1, u2 = z * s2;
+    const float f0 = floorf(u0), f1 = floorf(u1), f2 = floorf(u2);
+    const uint32_t x0 = min((uint32_t)f0, c0 - 1), x1 = min(x0 + 1, c0 - 1);
+    const uint32_t y0 = min((uint32_t)f1, c1 - 1), y1 = min(y0 + 1, c1 - 1);
+    const uint32_t z0 = min((uint32_t)f2, c2 - 1), z1 = min(z0 + 1, c2 - 1);
+    const float w0 = u0 - f0, w1 = u1 - f1, w2 = u2 - f2;
+    auto at = [&](uint32_t i, uint32_t j, uint32_t k) { return c[((uint64_t)i * c1 + j) * c2 + k]; };
+    auto line = [&](uint32_t i, uint32_t j) { return at(i, j, z0) * (1 - w2) + at(i, j, z1) * w2; };
+    const float a0 = line(x0, y0) * (1 - w1) + line(x0, y1) * w1;
+    const float a1 = line(x1, y0) * (1 - w1) + line(x1, y1) * w1;
+    return a0 * (1 - w0) + a1 * w0;
+}
+
+// One warp per fine block of bs^3 voxels: the mean over ns^3 evenly spread voxels of the
+// block of (fill_hi - fill_lo)^2, the squared difference between the trilinear fills of
+// two coarse passes over the same box -- the detail the finer pass adds there, a
+// predictor of the fill's error.  Blocks whose logit reaches logit_lo (when logits are
+// given, one per block) score +inf, so a top-k selection takes them first.
+__global__ void block_detail_kernel(const float *__restrict__ lo, uint32_t l0, uint32_t l1,
+                                    uint32_t l2, const float *__restrict__ hi, uint32_t h0,
+                                    uint32_t h1, uint32_t h2, uint32_t f0, uint32_t f1,
+                                    uint32_t f2, uint32_t bs, uint32_t ns, uint32_t b0,
+                                    uint32_t b1, uint32_t b2, const float *__restrict__ logits,
+                                    float logit_lo, float *__restrict__ out) {
+    const uint64_t nb = (uint64_t)b0 * b1 * b2;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    auto scale = [](uint32_t c, uint32_t f) { return f > 1 ? (float)(c - 1) / (float)(f - 1) : 0.0f; };
+    const float ls0 = scale(l0, f0), ls1 = scale(l1, f1), ls2 = scale(l2, f2);
+    const float hs0 = scale(h0, f0), hs1 = scale(h1, f1), hs2 = scale(h2, f2);
+    const uint32_t npts = ns * ns * ns;
+    for (uint64_t b = blockIdx.x * (uint64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); b < nb;
+         b += warps) {
+        const uint32_t bz = (uint32_t)(b % b2), by = (uint32_t)((b / b2) % b1),
+                       bx = (uint32_t)(b / ((uint64_t)b2 * b1));
+        float acc = 0.0f;
+        uint32_t cnt = 0;
+        for (uint32_t i = lane; i < npts; i += 32) {
+            // sample k of ns along an axis sits at (2k + 1) bs / (2 ns) inside the block
+            const uint32_t x = bx * bs + (2 * (i / (ns * ns)) + 1) * bs / (2 * ns);
+            const uint32_t y = by * bs + (2 * ((i / ns) % ns) + 1) * bs / (2 * ns);
+            const uint32_t z = bz * bs + (2 * (i % ns) + 1) * bs / (2 * ns);
+            if (x < f0 && y < f1 && z < f2) {
+                const float d = trilinear_at(hi, h0, h1, h2, hs0, hs1, hs2, x, y, z) -
+                                trilinear_at(lo, l0, l1, l2, ls0, ls1, ls2, x, y, z);
+                acc += d * d;
+                cnt++;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) {
+            float sc = cnt ? acc / (float)cnt : 0.0f;
+            if (!(sc >= 0.0f)) sc = 0.0f;  // NaN-safe: scores are non-negative
+            if (logits && logits[b] >= logit_lo) sc = INFINITY;
+            out[b] = sc;
+        }
+    }
+}
+
 __global__ void complex_abs_kernel(const float2 *__restrict__ in, uint64_t n,
                                    float *__restrict__ out) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -245,6 +312,30 @@ int bpgb_laplacian7(const float *d_volume, const uint32_t *voxels_per_side, floa
     if (total == 0) return BPGB_OK;
     const unsigned grid = (unsigned)((total + 255) / 256 < 152 * 16 ? (total + 255) / 256 : 152 * 16);
     laplacian7_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_volume, n[0], n[1], n[2], d_out);
+    count_launches(1);
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+int bpgb_block_detail(const float *d_coarse_lo, const uint32_t *lo_dims, const float *d_coarse_hi,
+                      const uint32_t *hi_dims, const uint32_t *fine_dims, uint32_t block_size,
+                      uint32_t samples, const float *d_logits, float logit_lo, float *d_score,
+                      void *stream) {
+    clear_error();
+    if (!d_coarse_lo || !lo_dims || !d_coarse_hi || !hi_dims || !fine_dims || !d_score ||
+        block_size == 0 || samples == 0 || samples > block_size)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad block_detail arguments");
+    for (int a = 0; a < 3; a++)
+        if (!lo_dims[a] || !hi_dims[a] || !fine_dims[a])
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "empty grid");
+    const uint32_t *f = fine_dims;
+    const uint32_t b0 = (f[0] + block_size - 1) / block_size, b1 = (f[1] + block_size - 1) / block_size,
+                   b2 = (f[2] + block_size - 1) / block_size;
+    const uint64_t nb = (uint64_t)b0 * b1 * b2;
+    const unsigned grid = (unsigned)((nb + 7) / 8 < 152 * 16 ? (nb + 7) / 8 : 152 * 16);
+    block_detail_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(
+        d_coarse_lo, lo_dims[0], lo_dims[1], lo_dims[2], d_coarse_hi, hi_dims[0], hi_dims[1],
+        hi_dims[2], f[0], f[1], f[2], block_size, samples, b0, b1, b2, d_logits, logit_lo, d_score);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;

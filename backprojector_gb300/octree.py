@@ -12,6 +12,13 @@ Pipeline for one capture (all on the GPU, no host synchronisation inside):
      block-sparse tile-list launch): p >= p_hi confident, p_lo <= p < p_hi the
      low-confidence band for which the dense pass is the fallback; p < p_lo keep step 3.
 
+Budgeted form (Reconstructor.reconstruct(budget=b)): a second coarse pass at 64^3 fills
+the skipped blocks instead, and the fine pass computes round(b x blocks) blocks: the
+CNN's blocks first, then the blocks where the 64^3 pass adds the most detail over the
+32^3 one (bpgb_block_detail, the predictor of the fill's error), selected on the device
+(bpgb_plan_select_tiles_topk).  Sweeping b gives the measured trade of speed against
+whole-volume error.
+
 Occupancy (labels and recall): voxel v of the dense reconstruction D is occupied when
 its negated 7-point Laplacian response F = -lap(D) (bpgb_laplacian7) reaches
 tau * max(F), tau = 0.2: the sharpened surfaces of the unfiltered backprojection, whose
@@ -234,7 +241,8 @@ class Reconstructor:
     back at the end of each pass)."""
 
     def __init__(self, geo: OctreeGeometry, device, fine_tile: int | None = 10,
-                 h_dtype: int = capi.DTYPE_F16, fine_splits: int = 8, **fine_opt):
+                 h_dtype: int = capi.DTYPE_F16, fine_splits: int = 8, fill: int | None = None,
+                 **fine_opt):
         import torch
 
         self.torch = torch
@@ -275,6 +283,17 @@ class Reconstructor:
         self.tile_count = torch.zeros(1, dtype=torch.int32, device=device)
         self.blocks = geo.coarse
         self.block_max = torch.empty(self.blocks, dtype=torch.float32, device=device)
+        # budgeted reconstructions: a second coarse pass at `fill`^3 fills the blocks the
+        # fine pass skips, and its detail over the 32^3 pass ranks the blocks
+        fill = 2 * geo.coarse[0] if fill is None else int(fill)
+        self.fill_dims = (fill, fill, fill)
+        n = geo.fine[0]
+        inc_fill = (np.asarray(geo.inc_fine, np.float64).reshape(3, 3) * (n - 1) / (fill - 1))
+        self.fill_plan = capi.Plan(geo.pairs, geo.T, self.fill_dims, geo.zero,
+                                   inc_fill.astype(np.float32).reshape(-1), geo.t0, geo.deltaT,
+                                   algo=capi.ALGO_FAST, h_dtype=h_dtype)
+        self.fill_vol = torch.empty(self.fill_dims, dtype=torch.float32, device=device)
+        self.score = torch.empty(self.blocks, dtype=torch.float32, device=device)
         self.X0 = torch.empty(int(np.prod(geo.coarse)) * 2, dtype=torch.bfloat16, device=device)
         self.logits = torch.empty(int(np.prod(geo.coarse)), dtype=torch.float32, device=device)
 
@@ -352,17 +371,34 @@ class Reconstructor:
         f = self._filtered(dense)
         return f >= tau * f.max()
 
-    def reconstruct(self, model: OccupancyCNN, logit_lo: float, out=None):
+    def reconstruct(self, model: OccupancyCNN, logit_lo: float, out=None,
+                    budget: float = 0.0):
         """Steps 1-4 of the module docstring on self.H, queued on self.stream (the
-        caller synchronises); returns the fine volume."""
+        caller synchronises); returns the fine volume.
+
+        budget > 0: a budgeted reconstruction.  The fill comes from the second coarse pass
+        (`fill`^3), and the fine pass computes the round(budget x blocks) blocks ranked
+        first -- the CNN's blocks (p >= p_lo) ahead of all others, then by the detail the
+        finer coarse pass adds over the 32^3 one (bpgb_block_detail), the predictor of
+        the fill's error; the k-th score is found on the device."""
         out = self.fine if out is None else out
         s = self.stream
         self.coarse_plan.execute(self.rows, self.coarse, s)
         model.features(self.coarse, self.geo.coarse, 1, self.X0, s)
         model.forward(self.X0, self.geo.coarse, 1, logits=self.logits, stream=s)
-        capi.upsample_trilinear(self.coarse, self.geo.coarse, out, self.geo.fine, s)
-        self.sparse_plan.select_tiles(self.logits, self.blocks, BLOCK, logit_lo, self.tile_list,
-                                      self.tile_count, s)
+        if budget > 0.0:
+            self.fill_plan.execute(self.rows, self.fill_vol, s)
+            capi.upsample_trilinear(self.fill_vol, self.fill_dims, out, self.geo.fine, s)
+            capi.block_detail(self.coarse, self.geo.coarse, self.fill_vol, self.fill_dims,
+                              self.geo.fine, BLOCK, self.score, d_logits=self.logits,
+                              logit_lo=logit_lo, stream=s)
+            k = int(round(min(budget, 1.0) * int(np.prod(self.blocks))))
+            self.sparse_plan.select_tiles_topk(self.score, self.blocks, BLOCK, k, self.tile_list,
+                                               self.tile_count, s)
+        else:
+            capi.upsample_trilinear(self.coarse, self.geo.coarse, out, self.geo.fine, s)
+            self.sparse_plan.select_tiles(self.logits, self.blocks, BLOCK, logit_lo,
+                                          self.tile_list, self.tile_count, s)
         self.sparse_plan.execute_tiles(self.rows, out, self.tile_list, self.tile_count,
                                        self.n_tiles, s)
         self._unscale(out)
@@ -376,7 +412,7 @@ class Reconstructor:
         return out
 
     def close(self):
-        for p in (self.coarse_plan, self.sparse_plan, self.label_plan):
+        for p in (self.coarse_plan, self.sparse_plan, self.label_plan, self.fill_plan):
             p.close()
 
 

@@ -245,9 +245,29 @@ def make_scene(spec: CaptureSpec, rng: np.random.Generator, lo: np.ndarray, hi: 
     return np.concatenate(pts).astype(np.float32), np.concatenate(alb).astype(np.float32)
 
 
+class ProductBackend:
+    """Host functions of a synthetic capture, from the product library: the volume basis
+    (bpgb_volume_basis), the renderer (bpgb_synth_render) and Poisson noise."""
+
+    @staticmethod
+    def volume_basis(volume_position, volume_size, voxels_per_side):
+        return capi.volume_basis(volume_position, volume_size, voxels_per_side)
+
+    @staticmethod
+    def render(pairs, T, t0, deltaT, points, albedo):
+        return capi.synth_render(pairs, T, t0, deltaT, points, albedo)
+
+    @staticmethod
+    def poisson(H, peak, seed):
+        return capi.synth_poisson(H, peak, seed)
+
+
 def make_capture(name: str, seed: int = 0, small: bool = False, render: bool = True,
-                 **overrides) -> Capture:
-    """Builds (and renders) a seeded capture of configuration `name`."""
+                 backend=None, **overrides) -> Capture:
+    """Builds (and renders) a seeded capture of configuration `name`.  `backend` supplies
+    volume_basis / render / poisson (default: the product library's); another backend
+    with the same arithmetic gives the same capture."""
+    be = backend or ProductBackend
     spec = SPECS[name]
     fields = dict(spec.__dict__)
     if small:
@@ -266,16 +286,16 @@ def make_capture(name: str, seed: int = 0, small: bool = False, render: bool = T
     vpos = np.asarray(spec.volume_position, np.float32)
     vsize = np.full(3, spec.volume_edge, np.float32)
     n = np.full(3, spec.voxels, np.uint32)
-    zero, inc = capi.volume_basis(vpos, vsize, n)
+    zero, inc = be.volume_basis(vpos, vsize, n)
     lo = vpos.astype(np.float64) - spec.volume_edge / 2
     hi = vpos.astype(np.float64) + spec.volume_edge / 2
     dT = float(np.float32(spec.deltaT))
     t0 = float(np.float32(math.floor(min_path(pairs, lo, hi) / dT) * dT))
     points, albedo = make_scene(spec, rng, lo, hi)
     if render:
-        H = capi.synth_render(pairs, spec.T, t0, dT, points, albedo)
+        H = be.render(pairs, spec.T, t0, dT, points, albedo)
         if spec.noise_peak:
-            capi.synth_poisson(H, spec.noise_peak, seed + 2)
+            be.poisson(H, spec.noise_peak, seed + 2)
     else:
         H = np.zeros((len(pairs), spec.T), np.float32)
     wl = None
@@ -295,7 +315,7 @@ BATCH_VOXELS = (32, 48, 64, 96)
 
 def make_batch(n: int = 64, seed: int = 0, render: bool = True, grids=BATCH_GRIDS,
                Ts=BATCH_T, voxels=BATCH_VOXELS, exhaustive_frac: float = 0.25,
-               exhaustive_grid: int = 16) -> list[Capture]:
+               exhaustive_grid: int = 16, backend=None) -> list[Capture]:
     """Seeded uneven batch: n captures with SPAD grids g^2 (g from `grids`), T from `Ts`,
     volumes v^3 (v from `voxels`) and 4-40 point scatterers each.
 
@@ -313,7 +333,7 @@ def make_batch(n: int = 64, seed: int = 0, render: bool = True, grids=BATCH_GRID
         v = int(rng.choice(voxels))
         k = int(rng.integers(4, 41))
         out.append(make_capture(
-            "dense_exhaustive_16", seed=seed * 1000 + i, render=render,
+            "dense_exhaustive_16", seed=seed * 1000 + i, render=render, backend=backend,
             laser_grid=(g, g) if exhaustive else None, spad_grid=(g, g), T=T, voxels=v,
             scene_params={"n": k, "albedo": (0.2, 1.0)}))
     return out

@@ -192,6 +192,15 @@ int bpgb_plan_execute_tiles(bpgb_plan plan, const void *d_H, void *d_volume,
 int bpgb_plan_select_tiles(bpgb_plan plan, const float *d_block_score,
                            const uint32_t *block_dims, uint32_t block_size, float threshold,
                            uint32_t *d_tile_list, uint32_t *d_tile_count, void *stream);
+/* Budgeted form of bpgb_plan_select_tiles: lists the tiles overlapping the k
+ * highest-scoring blocks (blocks tied with the k-th score included; scores are taken as
+ * non-negative, NaN as 0).  The k-th score is found on the device (radix selection, one
+ * CTA) and kept in the plan, so the call reads nothing on the host and can be captured
+ * in a CUDA graph; it zeroes *d_tile_count first and lists nothing when k = 0.  A plan
+ * must not run two selections concurrently. */
+int bpgb_plan_select_tiles_topk(bpgb_plan plan, const float *d_block_score,
+                                const uint32_t *block_dims, uint32_t block_size, uint32_t k,
+                                uint32_t *d_tile_list, uint32_t *d_tile_count, void *stream);
 /* Synchronises the plan's last stream and reports device-side diagnostics: returns
  * BPGB_ERR_TIMEOUT if a bounded wait gave up, BPGB_ERR_WINDOW if checked mode counted
  * out-of-window bins (count in *violations when non-null), else BPGB_OK. */
@@ -212,6 +221,21 @@ int bpgb_plan_dump_bins(bpgb_plan plan, const int64_t *h_voxel_ids, int64_t n,
 int bpgb_plan_get_tables(bpgb_plan plan, float *host_out, uint64_t capacity,
                          uint64_t *num_entries);
 int bpgb_plan_destroy(bpgb_plan plan);
+
+/* ---- FP64 evaluation of listed voxels (measurement) ----------------------------
+ * The reference kernel's quantity (backproject_cuda.cu:117-175) in double for the voxels
+ * d_voxel_ids[0..n) (linear ids, x slowest): voxel position, both legs, the bin
+ * round((d - t0) / deltaT) (half away from zero, kept in [0, T-1]) and the sum over
+ * pairs in pair order, every operation separately rounded.  For measuring the FP32
+ * paths' error on the GPU (the bench, tests); not a reconstruction path (one thread per
+ * voxel, FP64 pipes).  d_H: device rows [P, h_pitch] of float, or interleaved complex64
+ * when is_complex (h_pitch 0 = T, in elements); d_pairs: device pair list; d_out: device
+ * double[n] (complex: [n][2]).  Asynchronous on `stream`. */
+int bpgb_eval_f64_voxels(const void *d_H, int is_complex, uint32_t T, uint32_t h_pitch,
+                         const bpgb_pair *d_pairs, uint64_t num_pairs,
+                         const uint32_t *voxels_per_side, const float *volume_zero_pos,
+                         const float *voxel_inc, float t0, float deltaT,
+                         const int64_t *d_voxel_ids, int64_t n, double *d_out, void *stream);
 
 /* ---- allocation-free backprojection ----------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory
@@ -333,6 +357,16 @@ int bpgb_complex_abs(const float *d_in, uint64_t n, float *d_out, void *stream);
  * size / (n - 1) (the reference's voxel_inc, backproject.hpp:834-839). */
 int bpgb_upsample_trilinear(const float *d_coarse, const uint32_t *coarse_dims, float *d_fine,
                             const uint32_t *fine_dims, void *stream);
+/* Per-block predictor of the trilinear fill's error: for each block_size^3 block of the
+ * fine grid (float [ceil(f/bs)...], x slowest), the mean over samples^3 evenly spread
+ * voxels of (fill_hi - fill_lo)^2, where fill_* is the trilinear interpolation of two
+ * coarse passes over the same box (d_coarse_lo coarser than d_coarse_hi).  When d_logits
+ * (one per block) is given, blocks with logit >= logit_lo score +inf, so that
+ * bpgb_plan_select_tiles_topk takes the occupancy model's blocks first. */
+int bpgb_block_detail(const float *d_coarse_lo, const uint32_t *lo_dims, const float *d_coarse_hi,
+                      const uint32_t *hi_dims, const uint32_t *fine_dims, uint32_t block_size,
+                      uint32_t samples, const float *d_logits, float logit_lo, float *d_score,
+                      void *stream);
 
 /* Occupancy CNN kernels: 3x3x3 convolutions, zero padding, BF16 activations and weights,
  * FP32 accumulation on the tensor cores (mma.sync m16n8k16).  Activations are

@@ -440,3 +440,93 @@ void orc_precompute_distances(const float *laser_pos, const float *laser_grid, u
                 }
         }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Synthetic captures for the reference arm of the bench (not reference       */
+/* algorithms): the scene renderer and Poisson noise of the synthetic         */
+/* workloads, restated so that arm builds its inputs without the product      */
+/* library.  Same arithmetic as the product's host renderer, so the captures  */
+/* are identical bit for bit (tests/test_cpu.py checks it).                   */
+/* ------------------------------------------------------------------------- */
+
+/* H[p, b] += albedo / (|l - q|^2 |q - c|^2) for every scatterer q of pair p, b =
+ * round((lw + |l - q| + |q - c| + cw - t0) / dT), in FP64, scatterers in order. */
+void orc_synth_render(const orc_pair *pairs, uint64_t P, uint32_t T, float t0, float deltaT,
+                      const float *points, const float *albedo, uint64_t n, float *out)
+{
+    const double dT = deltaT;
+#pragma omp parallel
+    {
+        double *row = (double *)malloc(sizeof(double) * T);
+#pragma omp for schedule(dynamic, 8)
+        for (int64_t p = 0; p < (int64_t)P; p++) {
+            for (uint32_t t = 0; t < T; t++) row[t] = 0.0;
+            const orc_pair *pr = &pairs[p];
+            for (uint64_t i = 0; i < n; i++) {
+                const float *q = points + 3 * i;
+                double a2 = 0.0, b2 = 0.0;
+                for (int k = 0; k < 3; k++) {
+                    const double da = (double)pr->laser_point[k] - q[k];
+                    const double db = (double)q[k] - pr->camera_point[k];
+                    a2 += da * da;
+                    b2 += db * db;
+                }
+                const double d = (double)pr->laser_wall + sqrt(a2) + sqrt(b2) +
+                                 (double)pr->camera_wall;
+                const double b = round((d - (double)t0) / dT);
+                if (b < 0.0 || b >= (double)T || a2 <= 0.0 || b2 <= 0.0) continue;
+                row[(uint32_t)b] += (double)albedo[i] / (a2 * b2);
+            }
+            float *o = out + (uint64_t)p * T;
+            for (uint32_t t = 0; t < T; t++) o[t] = (float)row[t];
+        }
+        free(row);
+    }
+}
+
+static inline uint64_t orc_splitmix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+static inline double orc_uniform(uint64_t seed, uint64_t index, uint64_t draw)
+{
+    const uint64_t r = orc_splitmix64(seed ^ orc_splitmix64(index * 0x100000001B3ull + draw));
+    return ((double)(r >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+static double orc_poisson_sample(double lam, uint64_t seed, uint64_t index)
+{
+    if (!(lam > 0.0)) return 0.0;
+    if (lam < 30.0) {
+        const double L = exp(-lam);
+        double p = 1.0;
+        uint64_t k = 0;
+        do {
+            p *= orc_uniform(seed, index, k);
+            k++;
+        } while (p > L && k < 1000);
+        return (double)(k - 1);
+    }
+    const double u1 = orc_uniform(seed, index, 0), u2 = orc_uniform(seed, index, 1);
+    const double z = sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+    const double v = floor(lam + sqrt(lam) * z + 0.5);
+    return v > 0.0 ? v : 0.0;
+}
+
+/* H := Poisson(H * peak / max(H)) per bin, counter-based draws (seed, bin index). */
+void orc_synth_poisson(float *H, uint64_t n, float peak, uint64_t seed)
+{
+    if (!(peak > 0.0f) || n == 0) return;
+    float mx = 0.0f;
+#pragma omp parallel for reduction(max : mx)
+    for (int64_t i = 0; i < (int64_t)n; i++) mx = H[i] > mx ? H[i] : mx;
+    if (!(mx > 0.0f)) return;
+    const double scale = (double)peak / (double)mx;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++)
+        H[i] = (float)orc_poisson_sample((double)H[i] * scale, seed, (uint64_t)i);
+}

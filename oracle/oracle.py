@@ -64,6 +64,11 @@ def lib() -> C.CDLL:
         L.orc_precompute_distances.argtypes = [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
                                                C.c_uint32, C.c_int, _P]
         L.orc_precompute_distances.restype = None
+        L.orc_synth_render.argtypes = [_P, C.c_uint64, C.c_uint32, C.c_float, C.c_float, _F, _F,
+                                       C.c_uint64, _F]
+        L.orc_synth_render.restype = None
+        L.orc_synth_poisson.argtypes = [_F, C.c_uint64, C.c_float, C.c_uint64]
+        L.orc_synth_poisson.restype = None
         L.orc_num_threads.argtypes = []
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -268,3 +273,39 @@ def misbinned_fraction(bins_a, bins_b) -> float:
     """Fraction of (voxel, pair) updates whose bin (or in/out-of-range state) differs."""
     a, b = np.asarray(bins_a), np.asarray(bins_b)
     return float(np.mean(a != b))
+
+
+# ---------------------------------------------------------------- synthetic captures
+
+class SynthBackend:
+    """Host functions of a synthetic capture (volume basis, renderer, noise) without the
+    product library, for the bench's reference arm: the basis in FP32 numpy in the
+    product's operation order, the renderer and noise in oracle.c.  Identical captures
+    to the product's own (tests/test_cpu.py)."""
+
+    @staticmethod
+    def volume_basis(volume_position, volume_size, voxels_per_side):
+        pos = np.asarray(volume_position, np.float32)
+        size = np.asarray(volume_size, np.float32)
+        n = np.asarray(voxels_per_side, np.uint32)
+        zero = (pos - size / np.float32(2.0)).astype(np.float32)
+        inc = np.zeros(9, np.float32)
+        for a in range(3):
+            for k in range(3):
+                ax = np.float32(1.0 if a == k else 0.0)
+                inc[3 * a + k] = (ax * size[k]) / np.float32(int(n[k]) - 1)
+        return zero, inc
+
+    @staticmethod
+    def render(pairs, T, t0, deltaT, points, albedo):
+        pts = np.ascontiguousarray(points, np.float32)
+        alb = np.ascontiguousarray(albedo, np.float32)
+        out = np.zeros((len(pairs), T), np.float32)
+        lib().orc_synth_render(C.c_void_p(pairs.ctypes.data), len(pairs), T, t0, deltaT,
+                               _fp(pts), _fp(alb), len(alb), _fp(out))
+        return out
+
+    @staticmethod
+    def poisson(H, peak, seed):
+        lib().orc_synth_poisson(_fp(H), H.size, peak, seed)
+        return H

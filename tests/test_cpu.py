@@ -358,3 +358,16 @@ def test_bench_reference_arm_two_ranks():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+@pytest.mark.parametrize("name", ["dense_exhaustive_16", "precision_64", "octree_256"])
+def test_oracle_synth_backend_matches_product(name):
+    """The bench's reference arm builds its captures with oracle.SynthBackend (no product
+    library); they must equal the product backend's bit for bit (basis, rows, noise)."""
+    from backprojector_gb300 import synthetic
+
+    a = synthetic.make_capture(name, seed=13, small=True)
+    b = synthetic.make_capture(name, seed=13, small=True, backend=oracle.SynthBackend)
+    assert a.H.tobytes() == b.H.tobytes()
+    assert a.zero.tobytes() == b.zero.tobytes() and a.inc.tobytes() == b.inc.tobytes()
+    assert a.pairs.tobytes() == b.pairs.tobytes() and a.t0 == b.t0

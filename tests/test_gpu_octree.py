@@ -520,3 +520,147 @@ def test_phasor_octree_full_size(cuda):
     assert recall >= 0.99
     assert 0 < n_sel < 0.5 * po.n_tiles
     po.close()
+
+
+def test_topk_tile_selection_vs_numpy(cuda):
+    """bpgb_plan_select_tiles_topk lists exactly the tiles of the k highest-scoring
+    blocks (8^3 tiles on 8^3 blocks: one block per tile), ties and +inf included."""
+    import torch
+
+    c = synthetic.make_capture("precision_64", seed=2, small=True, render=False, voxels=64)
+    with capi.Plan(c.pairs, c.T, c.voxels_per_side, c.zero, c.inc, c.t0, c.deltaT,
+                   algo=capi.ALGO_FAST, tile=10) as plan:
+        nb = (8, 8, 8)
+        rng = np.random.default_rng(4)
+        score = rng.random(512).astype(np.float32)
+        score[rng.choice(512, 20, replace=False)] = np.inf
+        score[:5] = score[100]  # a tie
+        score[300:310] = 0.0
+        d_score = torch.from_numpy(score).to(cuda)
+        lst = torch.empty(512, dtype=torch.int32, device=cuda)
+        cnt = torch.zeros(1, dtype=torch.int32, device=cuda)
+        for k in (0, 1, 7, 20, 37, 200, 511, 512, 900):
+            plan.select_tiles_topk(d_score, nb, 8, k, lst, cnt)
+            torch.cuda.synchronize()
+            n = int(cnt.item())
+            got = set(int(t) for t in lst[:n].cpu().numpy())
+            if k == 0:
+                assert n == 0
+                continue
+            kth = np.sort(score)[::-1][min(k, 512) - 1]
+            # tile id t = (ty * tiles_x + tx) * tiles_z + tz; block id b = (bx * 8 + by) * 8 + bz
+            want = set()
+            for b in np.flatnonzero(score >= kth):
+                bx, by, bz = b // 64, (b // 8) % 8, b % 8
+                want.add(int((by * 8 + bx) * 8 + bz))
+            assert got == want, (k, len(got), len(want))
+
+
+def test_block_detail_vs_torch(cuda):
+    import torch
+    import torch.nn.functional as F
+
+    g = torch.Generator().manual_seed(3)
+    lo = torch.randn((4, 4, 4), generator=g)
+    hi = torch.randn((8, 8, 8), generator=g)
+    fine = (32, 32, 32)
+    out = torch.empty((4, 4, 4), device=cuda)
+    logits = torch.zeros(64)
+    logits[5] = 3.0
+    capi.block_detail(lo.to(cuda), (4, 4, 4), hi.to(cuda), (8, 8, 8), fine, 8, out, samples=4,
+                      d_logits=logits.to(cuda), logit_lo=1.0)
+    torch.cuda.synchronize()
+    fl = F.interpolate(lo[None, None], size=fine, mode="trilinear", align_corners=True)[0, 0]
+    fh = F.interpolate(hi[None, None], size=fine, mode="trilinear", align_corners=True)[0, 0]
+    pts = torch.tensor([1, 3, 5, 7])  # 4 samples per axis in an 8-voxel block
+    ref = torch.empty((4, 4, 4))
+    for bx in range(4):
+        for by in range(4):
+            for bz in range(4):
+                d = (fh - fl)[bx * 8 + pts][:, by * 8 + pts][:, :, bz * 8 + pts]
+                ref[bx, by, bz] = (d * d).mean()
+    got = out.cpu()
+    assert torch.isinf(got.reshape(-1)[5])
+    mask = torch.ones(64, dtype=torch.bool)
+    mask[5] = False
+    assert torch.allclose(got.reshape(-1)[mask], ref.reshape(-1)[mask], rtol=1e-4, atol=1e-6)
+
+
+def test_budgeted_reconstruction_limits(cuda):
+    """budget = 1 computes every block (equal to the dense pass bit for bit); a small
+    budget computes at least the CNN's blocks and fills the rest from the 64^3-style
+    second pass."""
+    import torch
+
+    geo = octree.OctreeGeometry.of("octree_256", small=True)
+    rec = octree.Reconstructor(geo, cuda, fine_tile=10)
+    model = octree.OccupancyCNN(cuda, seed=1)
+    rec.render(*octree.scene(geo, 9))
+    dense = rec.dense().clone()
+    out = rec.reconstruct(model, 1e30, budget=1.0)
+    rec.stream.synchronize()
+    assert torch.equal(out.clone(), dense)
+    assert rec.computed_mask().all()
+    out = rec.reconstruct(model, -1e30, budget=0.01)  # every block is a CNN block
+    rec.stream.synchronize()
+    assert rec.computed_mask().all()
+    out = rec.reconstruct(model, 1e30, budget=0.25).clone()
+    rec.stream.synchronize()
+    comp = rec.computed_mask()
+    nb = int(np.prod(rec.blocks))
+    assert int(rec.tile_count.item()) >= round(0.25 * nb)
+    assert torch.equal(out[comp], dense[comp])
+    rec.close()
+
+
+def test_trained_model_recall_vs_fp64_occupancy(cuda):
+    """Occupancy taken from FP64 values, not from an FP32 pass: the negated Laplacian of
+    the FP64 volume (bpgb_eval_f64_voxels, bit-identical to the FP64 oracle) on every voxel
+    whose FP32 response reaches 0.1 max and their face neighbours; the FP64-occupied voxels
+    (>= 0.2 of the FP64 maximum) are a subset of those candidates, since the FP32 and FP64
+    responses differ far less than 0.1 max.  The committed CNN backprojects >= 99% of them
+    at full resolution."""
+    import torch
+
+    model, state = octree.OccupancyCNN.load(cuda)
+    geo = octree.OctreeGeometry.of("octree_256")
+    rec = octree.Reconstructor(geo, cuda)
+    lo = octree.logit(float(state["p_lo"]))
+    n = geo.fine[0]
+    P = len(geo.pairs)
+    for seed in (3_000_004, 3_000_005):
+        rec.render(*octree.scene(geo, seed))
+        d32 = rec.dense_for_labels().clone()
+        f32 = torch.empty_like(d32)
+        capi.laplacian7(d32, geo.fine, f32)
+        cand = f32 >= 0.1 * f32.max()
+        near = cand.clone()
+        for ax in range(3):
+            near |= torch.roll(cand, 1, ax) | torch.roll(cand, -1, ax)
+        ids = torch.nonzero(near.reshape(-1)).reshape(-1)
+        d64 = torch.empty(len(ids), dtype=torch.float64, device=cuda)
+        capi.eval_f64_voxels(rec.H, geo.T, rec.d_pairs, P, geo.fine, geo.zero, geo.inc_fine,
+                             geo.t0, geo.deltaT, ids, d64)
+        vol64 = torch.zeros(n ** 3, dtype=torch.float64, device=cuda)
+        vol64[ids] = d64
+        vol64 = vol64.reshape(geo.fine)
+        lap = torch.zeros_like(vol64)
+        for ax in range(3):
+            for sh in (1, -1):
+                nb = torch.roll(vol64, sh, ax)
+                valid = torch.ones_like(vol64, dtype=torch.bool)
+                idx = [slice(None)] * 3
+                idx[ax] = 0 if sh == 1 else n - 1
+                valid[tuple(idx)] = False
+                lap += torch.where(valid, vol64 - nb, torch.zeros_like(vol64))
+        lap = torch.where(cand, lap, torch.full_like(lap, -np.inf))
+        occ64 = lap >= 0.2 * lap.max()
+        assert (f32[occ64] >= 0.15 * f32.max()).all()  # well inside the candidates
+        rec.reconstruct(model, lo)
+        rec.stream.synchronize()
+        comp = rec.computed_mask()
+        recall = float((comp & occ64).sum()) / max(1, int(occ64.sum()))
+        print(f"\n[octree_256 seed {seed}] recall of FP64-occupied voxels {recall:.5f} "
+              f"({int(occ64.sum())} voxels, {len(ids)} evaluated in FP64)")
+        assert recall >= 0.99
+    rec.close()
