@@ -131,6 +131,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_block_detail": (C.c_int, [_P, _U32, _P, _U32, _U32, C.c_uint32, C.c_uint32, _P,
                                     C.c_float, _P, _P]),
     "bpgb_plan_select_tiles_topk": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "bpgb_diag_mufu_rates": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "bpgb_set_dropin_algo": (C.c_int, [C.c_int]),
     "bpgb_get_dropin_algo": (C.c_int, []),
     "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -280,6 +281,13 @@ def pipe_rates() -> dict:
     r = (C.c_double * 3)()
     check(lib().bpgb_diag_pipe_rates(r), "bpgb_diag_pipe_rates")
     return {"rsqrt_per_sm_clk": r[0], "fp32_lanes_per_sm_clk": r[1], "lds_per_sm_clk": r[2]}
+
+
+def mufu_rates() -> dict:
+    """MUFU results per SM per clock, per operation (bpgb_diag_mufu_rates)."""
+    r = (C.c_double * 6)()
+    check(lib().bpgb_diag_mufu_rates(r, 6), "bpgb_diag_mufu_rates")
+    return dict(zip(("rsqrt_8_chains", "rsqrt_16_chains", "ex2", "sqrt", "rcp", "sin"), list(r)))
 
 
 def launch_count() -> int:

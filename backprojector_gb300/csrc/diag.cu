@@ -81,10 +81,102 @@ __global__ void __launch_bounds__(kProbeThreads) pipe_probe_kernel(int iters, Pr
     if (acc == -1.0f) out[blockIdx.x].sink = acc;  // keeps the chains live
 }
 
+// MUFU operations one at a time, in chains that stay bounded: OP 0 rsqrt x 8 chains,
+// 1 rsqrt x 16 chains, 2 ex2(-x), 3 sqrt, 4 rcp, 5 sin.  Same timing scheme as
+// pipe_probe_kernel; the per-SM rate is MUFU results per clock.
+template <int OP>
+__global__ void __launch_bounds__(kProbeThreads) mufu_probe_kernel(int iters, ProbeOut *out) {
+    constexpr int C = OP == 1 ? 16 : kChains;
+    float x[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) x[c] = 0.5f + 0.001f * (threadIdx.x + c);
+    __syncthreads();
+    const unsigned long long t0 = clock64();
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            float y;
+            if (OP <= 1) asm volatile("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
+            if (OP == 2) asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-x[c]));
+            if (OP == 3) asm volatile("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
+            if (OP == 4) asm volatile("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
+            if (OP == 5) asm volatile("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
+            x[c] = y;
+        }
+    }
+    __syncthreads();
+    const unsigned long long t1 = clock64();
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < C; c++) acc += x[c];
+    if (threadIdx.x == 0) {
+        out[blockIdx.x].cycles = t1 - t0;
+        out[blockIdx.x].sm = smid();
+    }
+    if (acc == -1.0f) out[blockIdx.x].sink = acc;
+}
+
+template <int OP>
+void launch_mufu_probe(int blocks, int iters, ProbeOut *d) {
+    mufu_probe_kernel<OP><<<blocks, kProbeThreads>>>(iters, d);
+}
+
+// Per-SM rate of a probe launch: (operations of the CTAs on an SM) / (its longest CTA's
+// cycles), averaged over SMs.
+double per_sm_rate(const std::vector<ProbeOut> &h, int sms, double ops_per_cta) {
+    std::vector<unsigned long long> longest(sms, 0);
+    std::vector<int> count(sms, 0);
+    for (const ProbeOut &o : h) {
+        if ((int)o.sm >= sms) continue;
+        longest[o.sm] = std::max(longest[o.sm], o.cycles);
+        count[o.sm]++;
+    }
+    double sum = 0.0;
+    int used = 0;
+    for (int s = 0; s < sms; s++)
+        if (count[s] && longest[s]) {
+            sum += (double)count[s] * ops_per_cta / (double)longest[s];
+            used++;
+        }
+    return used ? sum / used : 0.0;
+}
+
 }  // namespace
 }  // namespace bpgb
 
 using namespace bpgb;
+
+extern "C" int bpgb_diag_mufu_rates(double *rates, int n) {
+    clear_error();
+    if (!rates || n < 1) return set_error(BPGB_ERR_INVALID_ARGUMENT, "rates is null or n < 1");
+    int sms = 0;
+    int st = require_device(&sms);
+    if (st) return st;
+    const int blocks = sms * kProbeBlocksPerSm;
+    ProbeOut *d = nullptr;
+    BPGB_CUDA_TRY(cudaMalloc(&d, blocks * sizeof(ProbeOut)));
+    std::vector<ProbeOut> h(blocks);
+    const int iters = 2048;
+    void (*launch[6])(int, int, ProbeOut *) = {launch_mufu_probe<0>, launch_mufu_probe<1>,
+                                                launch_mufu_probe<2>, launch_mufu_probe<3>,
+                                                launch_mufu_probe<4>, launch_mufu_probe<5>};
+    for (int op = 0; op < 6 && op < n; op++) {
+        for (int rep = 0; rep < 2; rep++) {  // first launch warms up
+            launch[op](blocks, iters, d);
+            count_launches(1);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpy(h.data(), d, blocks * sizeof(ProbeOut), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return cuda_error(e, "mufu probe");
+        }
+        const double chains = op == 1 ? 16.0 : (double)kChains;
+        rates[op] = per_sm_rate(h, sms, (double)kProbeThreads * iters * chains);
+    }
+    cudaFree(d);
+    return BPGB_OK;
+}
 
 extern "C" int bpgb_diag_pipe_rates(double *rates) {
     clear_error();

@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "bpgb_internal.h"
@@ -61,48 +63,59 @@ __global__ void __launch_bounds__(kThreads)
 
 }  // namespace
 
+// Device copies of pulse taps, one per (taps, device), kept for the process: the
+// reconstruction path then neither allocates nor synchronises per call.
+int device_taps(const float *h_taps, int K, const float2 **out) {
+    static std::mutex mu;
+    struct Entry {
+        int dev;
+        std::vector<float2> taps;
+        float2 *d;
+    };
+    static std::vector<Entry> cache;
+    int dev = 0;
+    BPGB_CUDA_TRY(cudaGetDevice(&dev));
+    std::vector<float2> tp(K);
+    for (int k = 0; k < K; k++) tp[k] = make_float2(h_taps[k], h_taps[K + k]);
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry &e : cache)
+        if (e.dev == dev && e.taps.size() == tp.size() &&
+            std::memcmp(e.taps.data(), tp.data(), tp.size() * sizeof(float2)) == 0) {
+            *out = e.d;
+            return BPGB_OK;
+        }
+    float2 *d = nullptr;
+    BPGB_CUDA_TRY(cudaMalloc(&d, K * sizeof(float2)));
+    cudaError_t e = cudaMemcpy(d, tp.data(), K * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_error(e, "phasor taps upload");
+    }
+    cache.push_back({dev, std::move(tp), d});
+    *out = d;
+    return BPGB_OK;
+}
+
 int launch_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch,
                         const float *h_taps, int K, float *d_out, uint32_t out_pitch,
                         cudaStream_t stream) {
     if (rows == 0 || T == 0) return BPGB_OK;
     if (K <= 0) {
-        for (uint64_t r = 0; r < rows; r++)
-            BPGB_CUDA_TRY(cudaMemsetAsync(d_out + 2 * r * out_pitch, 0, (size_t)T * 8, stream));
+        BPGB_CUDA_TRY(cudaMemset2DAsync(d_out, (size_t)out_pitch * 8, 0, (size_t)T * 8, rows, stream));
         return BPGB_OK;
-    }
-    // taps as interleaved (cos, sin) pairs on the device (stream-ordered scratch)
-    std::vector<float2> tp(K);
-    for (int k = 0; k < K; k++) tp[k] = make_float2(h_taps[k], h_taps[K + k]);
-    float2 *d_taps = nullptr;
-    BPGB_CUDA_TRY(cudaMallocAsync(&d_taps, K * sizeof(float2), stream));
-    cudaError_t e = cudaMemcpyAsync(d_taps, tp.data(), K * sizeof(float2),
-                                    cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // tp is a host temporary
-    if (e != cudaSuccess) {
-        cudaFreeAsync(d_taps, stream);
-        return cuda_error(e, "phasor taps upload");
     }
     const uint32_t nseg = (T + kSeg - 1) / kSeg;
     const size_t smem = (size_t)(((kSeg + K + 1) & ~1) + 2 * K) * sizeof(float);
-    if (smem > 200 * 1024) {
-        cudaFreeAsync(d_taps, stream);
-        return set_error(BPGB_ERR_UNSUPPORTED, "phasor pulse too long for shared memory");
-    }
-    if (int rs = reserve_dynamic_smem((const void *)phasor_pulse_kernel, (uint32_t)smem)) {
-        cudaFreeAsync(d_taps, stream);
-        return rs;
-    }
+    if (smem > 200 * 1024) return set_error(BPGB_ERR_UNSUPPORTED, "phasor pulse too long for shared memory");
     const uint64_t blocks = rows * nseg;
-    if (blocks >= (1ull << 31)) {
-        cudaFreeAsync(d_taps, stream);
-        return set_error(BPGB_ERR_UNSUPPORTED, "too many rows for one launch");
-    }
+    if (blocks >= (1ull << 31)) return set_error(BPGB_ERR_UNSUPPORTED, "too many rows for one launch");
+    const float2 *d_taps = nullptr;
+    if (int st = device_taps(h_taps, K, &d_taps)) return st;
+    if (int rs = reserve_dynamic_smem((const void *)phasor_pulse_kernel, (uint32_t)smem)) return rs;
     phasor_pulse_kernel<<<(unsigned)blocks, kThreads, smem, stream>>>(
         d_H, T, in_pitch, d_taps, K, reinterpret_cast<float2 *>(d_out), out_pitch, nseg);
     count_launches(1);
-    e = cudaGetLastError();
-    cudaFreeAsync(d_taps, stream);
-    if (e != cudaSuccess) return cuda_error(e, "phasor pulse launch");
+    BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
 }
 

@@ -1002,6 +1002,137 @@ def roofline_for(achieved, ms, algo_bytes, phasor, clocks, dev, kernel, factored
     }
 
 
+PROFILE_CASES = ("dense256", "batch64", "octree", "cnn_train", "phasor128", "exhaustive32",
+                 "pulse128")
+
+
+def _timed(torch, stream, fn, reps):
+    ms = None
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+    return ms
+
+
+def run_profile_case(args):
+    """--profile-case NAME: a fixed launch sequence for profiling one kernel (ncu -k
+    <kernel> -s <n> -c 1), repeated --reps times (one to warm, one to capture); prints the
+    CUDA-event time of the last repetition.  Launch order per repetition (for ncu -s):
+      dense256: bp_fast_kernel x1;  batch64: bp_batch_kernel launches (+ split reductions);
+      phasor128: bp_fast_kernel, reduce_splits_kernel (pair splits > 1);
+      pulse128: phasor_pulse_kernel x1 (the 128^3 phasor capture's 16,384 rows);
+      exhaustive32: bp_fact_kernel (bp_fast_kernel with --unfactored), reduce_splits_kernel;
+      octree: bp_fast_kernel (coarse), conv_fwd_kernel x4, upsample, select_tiles,
+              bp_fast_kernel (tile list), scale;
+      cnn_train: conv_fwd x4, bce, conv_wgrad + reduce x4 interleaved with conv_fwd
+              (backward data) x3, adam x4, pack x4."""
+    from backprojector_gb300 import capi, octree, synthetic
+
+    args.tile = -1 if args.tile is None else args.tile
+    import torch
+
+    dev = torch.device("cuda:0")
+    s = torch.cuda.Stream()
+    out = {"case": args.profile_case}
+    if args.profile_case == "pulse128":
+        cap = synthetic.make_capture("phasor_128", seed=0)
+        dH = torch.from_numpy(cap.H).to(dev)
+        Hc = torch.empty(cap.H.shape, dtype=torch.complex64, device=dev)
+        out["ms"] = _timed(torch, s, lambda: capi.phasor_pulse_device(
+            dH, cap.P, cap.T, cap.T, cap.wavelength, cap.deltaT, Hc, cap.T, stream=s), args.reps)
+        out["taps"] = int(capi.phasor_taps(cap.wavelength, cap.deltaT).shape[1])
+        out["outputs"] = cap.P * cap.T
+    elif args.profile_case in ("dense256", "octree"):
+        geo = octree.OctreeGeometry.of("octree_256")
+        rec = octree.Reconstructor(geo, dev)
+        rec.render(*octree.scene(geo, 2_000_000))
+        if args.profile_case == "dense256":
+            f16 = args.dtype == "f16"
+            p = capi.Plan(geo.pairs, geo.T, geo.fine, geo.zero, geo.inc_fine, geo.t0, geo.deltaT,
+                          algo=capi.ALGO_FAST, tile=args.tile,
+                          h_dtype=capi.DTYPE_F16 if f16 else capi.DTYPE_F32)
+            rows = rec.rows if f16 else rec.H
+            out["ms"] = _timed(torch, s, lambda: p.execute(rows, rec.fine, s), args.reps)
+            out["plan"] = p.info()
+            out["updates"] = out["plan"]["updates"]
+            p.close()
+        else:
+            model, state = octree.OccupancyCNN.load(dev)
+            lo = octree.logit(float(state["p_lo"]))
+            out["ms"] = _timed(torch, rec.stream, lambda: rec.reconstruct(model, lo), args.reps)
+            out["selected_tiles"] = int(rec.tile_count.item())
+            out["tile"] = list(rec.tile)
+            out["updates_sparse"] = out["selected_tiles"] * int(np.prod(rec.tile)) * len(geo.pairs)
+        rec.close()
+    elif args.profile_case == "phasor128":
+        cap = synthetic.make_capture("phasor_128", seed=0)
+        Hc = torch.empty(cap.H.shape, dtype=torch.complex64, device=dev)
+        capi.phasor_pulse_device(torch.from_numpy(cap.H).to(dev), cap.P, cap.T, cap.T,
+                                 cap.wavelength, cap.deltaT, Hc, cap.T)
+        opt = dict(algo=capi.ALGO_FAST, tile=args.tile, chunk=args.chunk, stages=args.stages,
+                   pair_splits=args.splits, h_dtype=capi.DTYPE_C64)
+        rows = Hc
+        if args.dtype == "f16":
+            flat = torch.view_as_real(Hc)
+            scale = float(flat.abs().max()) / 16384.0 or 1.0
+            rows = (flat / scale).half().contiguous()
+            opt.update(h_dtype=capi.DTYPE_C32, h_scale=scale)
+        N = tuple(int(v) for v in cap.voxels_per_side)
+        dV = torch.empty(N, dtype=torch.complex64, device=dev)
+        torch.cuda.synchronize()
+        p = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT, **opt)
+        out["ms"] = _timed(torch, s, lambda: p.execute(rows, dV, s), args.reps)
+        out["plan"] = p.info()
+        p.close()
+    elif args.profile_case == "exhaustive32":
+        cap = synthetic.make_capture("dense_exhaustive_16", seed=0)
+        N = tuple(int(v) for v in cap.voxels_per_side)
+        dH = torch.from_numpy(cap.H).to(dev)
+        dV = torch.empty(N, dtype=torch.float32, device=dev)
+        p = capi.Plan(cap.pairs, cap.T, N, cap.zero, cap.inc, cap.t0, cap.deltaT,
+                      algo=capi.ALGO_FAST, tile=args.tile, chunk=args.chunk, stages=args.stages,
+                      pair_splits=args.splits, unfactored=int(args.unfactored))
+        torch.cuda.synchronize()
+        out["ms"] = _timed(torch, s, lambda: p.execute(dH, dV, s), args.reps)
+        out["plan"] = p.info()
+        p.close()
+    elif args.profile_case == "batch64":
+        caps = synthetic.make_batch(64, seed=0)
+        scales = synthetic.fp16_scales(caps)
+        b = capi.Batch(synthetic.batch_geometry(caps, scales), h_dtype=capi.DTYPE_F16,
+                       unfactored=int(args.unfactored))
+        info = b.info()
+        H = synthetic.pack_batch(caps, b.row_offsets, info["pitch"], np.float16, scales)
+        dH = torch.from_numpy(H).to(dev)
+        dV = torch.empty(info["total_voxels"], device=dev)
+        out["ms"] = _timed(torch, s, lambda: b.execute(dH, dV, s), args.reps)
+        out["batch"] = info
+        b.close()
+    else:
+        geo = octree.OctreeGeometry.of("octree_256")
+        rec = octree.Reconstructor(geo, dev)
+        n = 16
+        coarse = torch.empty((n, int(np.prod(geo.coarse))), device=dev)
+        bnorm = torch.empty_like(coarse)
+        for i in range(n):
+            rec.render(*octree.scene(geo, 1_000_000 + i))
+            coarse[i] = rec.coarse_pass().reshape(-1)
+            bnorm[i] = rec.labels_from_dense(rec.dense_for_labels()).reshape(-1)
+        rec.close()
+        model = octree.OccupancyCNN(dev, seed=0)
+        X = model.features(coarse, geo.coarse, n)
+        y = (bnorm >= octree.TAU).to(torch.uint8).reshape(-1).contiguous()
+        torch.cuda.synchronize()
+        out["ms"] = _timed(torch, torch.cuda.current_stream(),
+                           lambda: model.train_step(X, y, geo.coarse, n, 1e-3, 50.0), args.reps)
+        out["voxels"] = n * int(np.prod(geo.coarse))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1030,8 +1161,17 @@ def main():
     ap.add_argument("--no-octree", action="store_true",
                     help="octree_256: skip the learned-octree object of the line")
     ap.add_argument("--no-ref-gpu", action="store_true", help="accepted for compatibility")
+    ap.add_argument("--profile-case", choices=PROFILE_CASES, default=None,
+                    help="run a fixed launch sequence for ncu instead of the bench")
+    ap.add_argument("--reps", type=int, default=2, help="--profile-case repetitions")
+    ap.add_argument("--chunk", type=int, default=0, help="--profile-case: rows per stage")
+    ap.add_argument("--stages", type=int, default=0, help="--profile-case: pipeline depth")
+    ap.add_argument("--splits", type=int, default=0, help="--profile-case: pair splits")
+    ap.add_argument("--unfactored", action="store_true", help="--profile-case: per-pair legs")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference_arm(args)
     elif args.workload == "batch_64":
         run_batch(args)

@@ -490,12 +490,20 @@ int bpgb_diag_wait_timeout(uint32_t spin_limit);
  * results (XU pipe), rates[1] FP32 lanes of packed FP32x2 FMAs, rates[2] conflict-free
  * 32-bit shared-memory loads.  The roofline of the FAST update is derived from these. */
 int bpgb_diag_pipe_rates(double *rates);
+/* MUFU (special-function unit) results per SM per clock, measured one operation at a
+ * time on the current device: rates[0] rsqrt.approx with 8 independent chains per
+ * thread, [1] rsqrt.approx with 16, [2] ex2.approx, [3] sqrt.approx, [4] rcp.approx,
+ * [5] sin.approx (the first n of them).  For the roofline of the FAST kernel, whose
+ * update costs one rsqrt. */
+int bpgb_diag_mufu_rates(double *rates, int n);
 
 /* ---- phasor pulse --------------------------------------------------------
  * d_out[r, t] = sum_k d_H[r, t + k - K/2] * (cos_k, sin_k), read index in (0, T), with
  * K = int(times * wavelength / deltaT) taps built as the reference does (FP64 Gaussian
  * and phase, rounded to FP32).  d_H: float [rows, in_pitch]; d_out: interleaved
- * complex64 [rows, out_pitch].  Asynchronous on stream. */
+ * complex64 [rows, out_pitch].  Asynchronous on stream; the first call for a given
+ * (wavelength, deltaT, times) on a device uploads the taps once (a small synchronous
+ * allocation kept until exit), later calls allocate nothing. */
 int bpgb_phasor_pulse(const float *d_H, uint64_t rows, uint32_t T, uint32_t in_pitch,
                       float wavelength, float deltaT, uint32_t times, float *d_out,
                       uint32_t out_pitch, void *stream);
