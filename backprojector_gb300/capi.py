@@ -148,6 +148,8 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_volume_basis": (C.c_int, [_F, _F, _U32, _F, _F, _F]),
     "bpgb_time_limits": (C.c_int, [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
                                    C.c_uint32, _F, _F, C.c_float, C.c_float, _F, _F]),
+    "bpgb_time_limits_corners": (C.c_int, [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
+                                   C.c_uint32, _F, _F, C.c_float, C.c_float, _F, _F]),
     "bpgb_backproject_capture": (C.c_int, [_F, C.c_uint32, _F, C.c_uint32, C.c_uint32, _F,
                                            C.c_uint32, C.c_uint32, _F, _F, C.c_float, C.c_float,
                                            C.c_int, _F, _F, _U32, _F, C.c_int,
@@ -308,13 +310,16 @@ def volume_basis(volume_position, volume_size, voxels_per_side, wall_normal=(0, 
 
 
 def time_limits(laser_position, laser_grid, camera_position, camera_grid, volume_position,
-                volume_size, t0, deltaT):
+                volume_size, t0, deltaT, corners: bool = False):
+    """(min, max) fractional bin limits: over every grid point (default) or the
+    reference's corner bound (corners=True, bpgb_time_limits_corners)."""
     lg, cg = f32(laser_grid), f32(camera_grid)
     mn, mx = C.c_float(), C.c_float()
-    check(lib().bpgb_time_limits(fptr(f32(laser_position)), fptr(lg), lg.shape[0], lg.shape[1],
-                                 fptr(f32(camera_position)), fptr(cg), cg.shape[0], cg.shape[1],
-                                 fptr(f32(volume_position)), fptr(f32(volume_size)), t0, deltaT,
-                                 C.byref(mn), C.byref(mx)), "bpgb_time_limits")
+    name = "bpgb_time_limits_corners" if corners else "bpgb_time_limits"
+    check(getattr(lib(), name)(fptr(f32(laser_position)), fptr(lg), lg.shape[0], lg.shape[1],
+                               fptr(f32(camera_position)), fptr(cg), cg.shape[0], cg.shape[1],
+                               fptr(f32(volume_position)), fptr(f32(volume_size)), t0, deltaT,
+                               C.byref(mn), C.byref(mx)), name)
     return mn.value, mx.value
 
 

@@ -31,18 +31,22 @@ struct Window {
     float M;        // fractional last index from the time limits
 };
 
+// corners: the reference's corner-point bound (bpgb_time_limits_corners) instead of the
+// bound over every grid point (bpgb_time_limits).
 int capture_window(const float *laser_grid, uint32_t lx, uint32_t ly, const float *camera_grid,
                    uint32_t cx, uint32_t cy, const float *camera_position,
                    const float *laser_position, float t0, float deltaT, int confocal,
-                   const float *volume_position, const float *volume_size, Window *w) {
+                   const float *volume_position, const float *volume_size, Window *w,
+                   bool corners = false) {
     float mn = 0, mx = 0;
     // Confocal captures illuminate the camera grid from the camera position: both legs
     // are |camera_position - c| (backproject.hpp:405-411).
     const float *lg = confocal ? camera_grid : laser_grid;
     const float *lp = confocal ? camera_position : laser_position;
     const uint32_t glx = confocal ? cx : lx, gly = confocal ? cy : ly;
-    int st = bpgb_time_limits(lp, lg, glx, gly, camera_position, camera_grid, cx, cy,
-                              volume_position, volume_size, t0, deltaT, &mn, &mx);
+    int st = (corners ? bpgb_time_limits_corners : bpgb_time_limits)(
+        lp, lg, glx, gly, camera_position, camera_grid, cx, cy, volume_position, volume_size,
+        t0, deltaT, &mn, &mx);
     if (st) return st;
     const double lo = std::floor((double)mn), hi = std::ceil((double)mx);
     if (!(hi > lo) || hi - lo > 1e8)
@@ -80,7 +84,7 @@ int prepare(const float *camera_grid, uint32_t cx, uint32_t cy, const float *las
             uint32_t lx, uint32_t ly, const float *camera_position, const float *laser_position,
             float t0, float deltaT, int confocal, const float *volume_position,
             const float *volume_size, const uint32_t *voxels_per_side, const float *wall_normal,
-            Common *c) {
+            Common *c, bool corners = false) {
     if (!camera_grid || !camera_position || !volume_position || !volume_size || !voxels_per_side)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "null capture argument");
     if (!confocal && (!laser_grid || !laser_position))
@@ -90,7 +94,7 @@ int prepare(const float *camera_grid, uint32_t cx, uint32_t cy, const float *las
     const float zeros3[3] = {0, 0, 0};
     const float *lpos = laser_position ? laser_position : zeros3;
     int st = capture_window(laser_grid, lx, ly, camera_grid, cx, cy, camera_position, lpos, t0,
-                            deltaT, confocal, volume_position, volume_size, &c->w);
+                            deltaT, confocal, volume_position, volume_size, &c->w, corners);
     if (st) return st;
     c->P = confocal ? (uint64_t)cx * cy : (uint64_t)lx * ly * cx * cy;
     c->pairs.resize(c->P);
@@ -115,12 +119,15 @@ int bpgb_capture_window(const float *camera_grid, uint32_t cx, uint32_t cy,
     if (!camera_grid || !camera_position || !volume_position || !volume_size || !from || !len ||
         !chunk_t0 || (!confocal && (!laser_grid || !laser_position)))
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "null capture argument");
-    if (t0_mode < 0 || t0_mode > 2) return set_error(BPGB_ERR_INVALID_ARGUMENT, "t0_mode 0, 1 or 2");
+    if ((t0_mode & ~4) < 0 || (t0_mode & ~4) > 2)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "t0_mode 0, 1 or 2, plus 4 for corner limits");
+    const bool corners = (t0_mode & 4) != 0;
+    t0_mode &= ~4;
     const float zeros3[3] = {0, 0, 0};
     Window w;
     int st = capture_window(laser_grid, lx, ly, camera_grid, cx, cy, camera_position,
                             laser_position ? laser_position : zeros3, t0, deltaT, confocal,
-                            volume_position, volume_size, &w);
+                            volume_position, volume_size, &w, corners);
     if (st) return st;
     if (t0_mode == 2) {  // phasor: int limits (backproject.hpp:962)
         const int mi = (int)w.m, Mi = (int)w.M;
@@ -147,11 +154,16 @@ int bpgb_backproject_capture(const float *transient_data, uint32_t T,
     clear_error();
     if (!transient_data || !out_volume || T == 0)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "null transient data / output or T == 0");
+    if ((t0_mode & ~4) < 0 || (t0_mode & ~4) > 1)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "t0_mode 0 or 1, plus 4 for corner limits");
+    const bool corners = (t0_mode & 4) != 0;
+    t0_mode &= ~4;
     int st = require_device();
     if (st) return st;
     Common c;
     st = prepare(camera_grid, cx, cy, laser_grid, lx, ly, camera_position, laser_position, t0,
-                 deltaT, confocal, volume_position, volume_size, voxels_per_side, wall_normal, &c);
+                 deltaT, confocal, volume_position, volume_size, voxels_per_side, wall_normal, &c,
+                 corners);
     if (st) return st;
     bpgb_options o;
     bpgb_options_default(&o);

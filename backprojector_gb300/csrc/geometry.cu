@@ -240,4 +240,71 @@ int bpgb_time_limits(const float *laser_position, const float *laser_grid, uint3
     return BPGB_OK;
 }
 
+int bpgb_time_limits_corners(const float *laser_position, const float *laser_grid, uint32_t lx,
+                             uint32_t ly, const float *camera_position, const float *camera_grid,
+                             uint32_t cx, uint32_t cy, const float *volume_position,
+                             const float *volume_size, float t0, float deltaT, float *min_index,
+                             float *max_index) {
+    // get_time_limits (backproject.hpp:617-674) as written: the 4 corner points of each
+    // grid (get_nd_corners / get_corner, :490-547), the 8 corners of the volume box
+    // position - size / 2 + {0, 1} size (:513-569), min / max of bp::distance (FP32
+    // points, FP64 differences and sum, :42-53) between origin and grid corners and
+    // between volume corners and grid corners (get_min_max_distances, :580-598, kept
+    // in float), the four minima (maxima) summed in float, minus t0, over deltaT, padded
+    // by 100 bins.  The reference transposes the camera grid in the row-major case
+    // (:651-652), which under xtensor's slicing rules does not yield the grid's corner
+    // points; the grid's 4 corners are used here.
+    clear_error();
+    if (!laser_position || !laser_grid || !camera_position || !camera_grid || !volume_position ||
+        !volume_size || !min_index || !max_index || lx == 0 || ly == 0 || cx == 0 || cy == 0)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad time-limit arguments");
+    if (!(deltaT > 0.0f)) return set_error(BPGB_ERR_INVALID_ARGUMENT, "deltaT must be > 0");
+    auto dist = [](const float *a, const float *b) {
+        double t[3];
+        for (int k = 0; k < 3; k++) {
+            t[k] = (double)a[k] - (double)b[k];
+            t[k] = t[k] * t[k];
+        }
+        return std::sqrt(t[0] + t[1] + t[2]);
+    };
+    // corner i of a [gx, gy, 3] grid: bit 1 of i selects the last row, bit 0 the last column
+    auto grid_corners = [](const float *g, uint32_t gx, uint32_t gy, float out[4][3]) {
+        for (int i = 0; i < 4; i++) {
+            const uint32_t a = (i & 2) ? gx - 1 : 0, b = (i & 1) ? gy - 1 : 0;
+            for (int k = 0; k < 3; k++) out[i][k] = g[3 * ((uint64_t)a * gy + b) + k];
+        }
+    };
+    float las[4][3], cam[4][3], vol[8][3];
+    grid_corners(laser_grid, lx, ly, las);
+    grid_corners(camera_grid, cx, cy, cam);
+    for (int i = 0; i < 8; i++)
+        for (int k = 0; k < 3; k++) {
+            const float lower = volume_position[k] - volume_size[k] / 2.0f;
+            const float m = (i & (1 << (2 - k))) ? 1.0f : 0.0f;
+            vol[i][k] = lower + m * volume_size[k];
+        }
+    auto minmax = [&](const float (*A)[3], int na, const float (*B)[3], int nb, float &mn, float &mx) {
+        mn = std::numeric_limits<float>::max();
+        mx = 0.0f;
+        for (int i = 0; i < na; i++)
+            for (int j = 0; j < nb; j++) {
+                const float d = (float)dist(A[i], B[j]);
+                mn = std::min(d, mn);
+                mx = std::max(d, mx);
+            }
+    };
+    float a0, a1, b0, b1, c0, c1, d0, d1;
+    minmax((const float(*)[3])laser_position, 1, las, 4, a0, a1);
+    minmax((const float(*)[3])camera_position, 1, cam, 4, b0, b1);
+    minmax(vol, 8, las, 4, c0, c1);
+    minmax(vol, 8, cam, 4, d0, d1);
+    float mn = a0 + b0 + c0 + d0;
+    float mx = a1 + b1 + c1 + d1;
+    mn -= t0;
+    mx -= t0;
+    *min_index = mn / deltaT - 100;
+    *max_index = mx / deltaT + 100;
+    return BPGB_OK;
+}
+
 }  // extern "C"

@@ -530,13 +530,28 @@ int bpgb_time_limits(const float *laser_position, const float *laser_grid, uint3
                      uint32_t cx, uint32_t cy, const float *volume_position,
                      const float *volume_size, float t0, float deltaT, float *min_index,
                      float *max_index);
+/* The reference's own bound (get_time_limits, backproject.hpp:617-674): distances
+ * between the 4 corner points of each grid, the origins and the 8 corners of the volume
+ * box, in FP64 per distance, summed in FP32, minus t0, over deltaT, padded by 100 bins.
+ * Corners can miss the shortest paths through interior grid points, which the padding
+ * usually covers.  The reference transposes the camera grid first in the row-major case
+ * (:651-652); under xtensor's slicing rules that does not select the grid's corner
+ * points, and xtensor is not available to reproduce it, so the grid's own 4 corners are
+ * taken.  Selected in the capture calls by t0_mode + 4. */
+int bpgb_time_limits_corners(const float *laser_position, const float *laser_grid, uint32_t lx,
+                             uint32_t ly, const float *camera_position, const float *camera_grid,
+                             uint32_t cx, uint32_t cy, const float *volume_position,
+                             const float *volume_size, float t0, float deltaT, float *min_index,
+                             float *max_index);
 
 /* ---- time window on device-resident captures ------------------------------
  * The window bp::backproject / bp::phasor_reconstruction crop a capture to
  * (get_time_limits + get_transient_chunk, backproject.hpp:617-740): original bins
  * [*from, *from + *len) (from may be negative: zero-padded) and the chunk's t0 for
  * t0_mode 0 (dense, the reference's unfloored offset, :847), 1 (floored offset) or 2
- * (phasor: limits truncated to int, :962).  bpgb_rows_crop copies that window of device
+ * (phasor: limits truncated to int, :962); adding 4 takes the limits from the reference's
+ * corner bound (bpgb_time_limits_corners) instead of the bound over every grid point
+ * (bpgb_time_limits).  bpgb_rows_crop copies that window of device
  * rows [rows][in_pitch] into [rows][out_pitch] (zeros outside [0, T) and past len) on
  * `stream`, so a device-resident capture is cropped without a host round trip; a plan
  * with T = len, h_pitch = out_pitch and t0 = *chunk_t0 then reproduces
@@ -555,7 +570,9 @@ int bpgb_rows_crop(const float *d_in, uint64_t rows, uint32_t T, uint32_t in_pit
  * precompute, basis, then the backprojection.  transient_data is row-major
  * [lx, ly, cx, cy, T] (exhaustive) or [cx, cy, T] (confocal).  t0_mode 0 keeps the
  * reference's fractional chunk offset (chunked_t0 = t0 + m*deltaT with m unfloored),
- * 1 uses the floored offset (no sub-bin shift).  Output [Nx, Ny, Nz] float, or
+ * 1 uses the floored offset (no sub-bin shift); + 4 takes m from the reference's corner
+ * bound (t0_mode 4: the reference's semantics, 5: its corners with the floored offset).
+ * Output [Nx, Ny, Nz] float, or
  * interleaved complex64 for the phasor call. */
 int bpgb_backproject_capture(const float *transient_data, uint32_t T,
                              const float *camera_grid, uint32_t cx, uint32_t cy,

@@ -530,3 +530,66 @@ void orc_synth_poisson(float *H, uint64_t n, float peak, uint64_t seed)
     for (int64_t i = 0; i < (int64_t)n; i++)
         H[i] = (float)orc_poisson_sample((double)H[i] * scale, seed, (uint64_t)i);
 }
+
+/* ------------------------------------------------------------------------- */
+/* get_time_limits (backproject.hpp:617-674) with its corner semantics:       */
+/* get_corner / get_nd_corners (:490-569), get_min_max_distances (:580-598),  */
+/* bp::distance (:42-53).  Grid corner i: bit 1 -> last row, bit 0 -> last    */
+/* column (mask & 1 << (ndim - 1 - dim)); volume corner i: bit (2 - k) adds   */
+/* size[k] to position[k] - size[k] / 2.  The camera-grid transpose of the    */
+/* row-major case (:651-652) is not reproduced (xtensor slicing semantics).   */
+/* ------------------------------------------------------------------------- */
+static double orc_ref_distance(const float *p1, const float *p2)
+{
+    double t[3];
+    for (int i = 0; i < 3; i++) {
+        t[i] = (double)p1[i] - (double)p2[i];
+        t[i] = t[i] * t[i];
+    }
+    return sqrt(t[0] + t[1] + t[2]);
+}
+
+static void orc_minmax(const float *A, int na, const float *B, int nb, float *mn, float *mx)
+{
+    float lo = 3.402823466e+38f, hi = 0.0f;
+    for (int i = 0; i < na; i++)
+        for (int j = 0; j < nb; j++) {
+            float d = (float)orc_ref_distance(A + 3 * i, B + 3 * j);
+            lo = d < lo ? d : lo;
+            hi = d > hi ? d : hi;
+        }
+    *mn = lo;
+    *mx = hi;
+}
+
+void orc_time_limits_corners(const float *laser_pos, const float *laser_grid, uint32_t lx,
+                             uint32_t ly, const float *camera_pos, const float *camera_grid,
+                             uint32_t cx, uint32_t cy, const float *vol_pos,
+                             const float *vol_size, float t0, float dT, float *out)
+{
+    float las[12], cam[12], vol[24];
+    for (int i = 0; i < 4; i++) {
+        uint32_t a = (i & 2) ? lx - 1 : 0, b = (i & 1) ? ly - 1 : 0;
+        uint32_t c = (i & 2) ? cx - 1 : 0, d = (i & 1) ? cy - 1 : 0;
+        for (int k = 0; k < 3; k++) {
+            las[3 * i + k] = laser_grid[3 * ((uint64_t)a * ly + b) + k];
+            cam[3 * i + k] = camera_grid[3 * ((uint64_t)c * cy + d) + k];
+        }
+    }
+    for (int i = 0; i < 8; i++)
+        for (int k = 0; k < 3; k++) {
+            float lower = vol_pos[k] - vol_size[k] / 2.0f;
+            float m = (i & (1 << (2 - k))) ? 1.0f : 0.0f;
+            vol[3 * i + k] = lower + m * vol_size[k];
+        }
+    float a0, a1, b0, b1, c0, c1, d0, d1;
+    orc_minmax(laser_pos, 1, las, 4, &a0, &a1);
+    orc_minmax(camera_pos, 1, cam, 4, &b0, &b1);
+    orc_minmax(vol, 8, las, 4, &c0, &c1);
+    orc_minmax(vol, 8, cam, 4, &d0, &d1);
+    float mn = a0 + b0 + c0 + d0, mx = a1 + b1 + c1 + d1;
+    mn -= t0;
+    mx -= t0;
+    out[0] = mn / dT - 100;
+    out[1] = mx / dT + 100;
+}

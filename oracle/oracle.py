@@ -69,6 +69,9 @@ def lib() -> C.CDLL:
         L.orc_synth_render.restype = None
         L.orc_synth_poisson.argtypes = [_F, C.c_uint64, C.c_float, C.c_uint64]
         L.orc_synth_poisson.restype = None
+        L.orc_time_limits_corners.argtypes = [_F, _F, C.c_uint32, C.c_uint32, _F, _F, C.c_uint32,
+                                              C.c_uint32, _F, _F, C.c_float, C.c_float, _F]
+        L.orc_time_limits_corners.restype = None
         L.orc_num_threads.argtypes = []
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -309,3 +312,15 @@ class SynthBackend:
     def poisson(H, peak, seed):
         lib().orc_synth_poisson(_fp(H), H.size, peak, seed)
         return H
+
+
+def time_limits_corners(laser_position, laser_grid, camera_position, camera_grid,
+                        volume_position, volume_size, t0, deltaT):
+    """get_time_limits (backproject.hpp:617-674) with its corner bound: (min, max) bins."""
+    lg, cg = _f32(laser_grid), _f32(camera_grid)
+    out = np.zeros(2, np.float32)
+    lib().orc_time_limits_corners(_fp(_f32(laser_position)), _fp(lg), lg.shape[0], lg.shape[1],
+                                  _fp(_f32(camera_position)), _fp(cg), cg.shape[0], cg.shape[1],
+                                  _fp(_f32(volume_position)), _fp(_f32(volume_size)), t0, deltaT,
+                                  _fp(out))
+    return float(out[0]), float(out[1])

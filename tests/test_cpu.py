@@ -296,6 +296,29 @@ def test_capture_window_matches_time_limits():
     assert fr2 == int(m) and ln2 == int(M) - int(m)
     with pytest.raises(capi.BackprojectorError):
         capi.capture_window(*args, t0_mode=3)
+    # + 4: the reference's corner bound
+    mc, Mc = capi.time_limits(c.laser_position, c.laser_grid, c.camera_position, c.camera_grid,
+                              c.volume_position, c.volume_size, c.t0, c.deltaT, corners=True)
+    fr4, ln4, ct4 = capi.capture_window(*args, t0_mode=4)
+    assert fr4 == int(np.floor(mc)) and ln4 == int(np.ceil(Mc)) - int(np.floor(mc))
+    assert ct4 == float(np.float32(c.t0) + np.float32(mc) * np.float32(c.deltaT))
+
+
+@pytest.mark.parametrize("name", ["dense_exhaustive_16", "precision_64", "octree_256", "phasor_128"])
+def test_time_limits_corners_match_oracle(name):
+    """bpgb_time_limits_corners restates get_time_limits (backproject.hpp:617-674) with its
+    corner semantics; the oracle's restatement gives the same floats."""
+    for small in (True, False):
+        c = synthetic.make_capture(name, small=small, render=False)
+        args = (c.laser_position, c.laser_grid, c.camera_position, c.camera_grid,
+                c.volume_position, c.volume_size, c.t0, c.deltaT)
+        got = capi.time_limits(*args, corners=True)
+        want = oracle.time_limits_corners(*args)
+        assert np.float32(got[0]) == np.float32(want[0]) and np.float32(got[1]) == np.float32(want[1])
+        # the bound over every grid point and the volume box is never looser on the low side
+        # by more than the grids' corner geometry allows: both cover [t0-relative min, max]
+        m, M = capi.time_limits(*args)
+        assert m < M and got[0] < got[1]
 
 
 def _max_worker(rank, world, port, q):
