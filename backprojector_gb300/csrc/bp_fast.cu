@@ -2113,6 +2113,8 @@ struct BatchPlan {
     unsigned long long *d_diag = nullptr;
     unsigned int *d_sched = nullptr;  // work counter, finished-CTA counter
     cudaStream_t own_stream = nullptr;
+    cudaStream_t side_stream = nullptr;  // the per-pair launch when both kinds run
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t graph = nullptr;
     const void *graph_H = nullptr;
     const float *graph_out = nullptr;
@@ -2123,6 +2125,9 @@ void batch_free(BatchPlan *b) {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    if (b->side_stream) cudaStreamDestroy(b->side_stream);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     cudaFree(b->d_caps);
     cudaFree(b->d_units);
     cudaFree(b->d_tables);
@@ -2145,10 +2150,21 @@ int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (batch)");
-    for (int f = 0; f < 2; f++) {
-        const uint32_t n_pp = b->n_units - b->n_fact;
+    // With both kinds of capture the two persistent launches run concurrently: the
+    // factored launch (most of the work) on `s`, the per-pair launch on the batch's side
+    // stream forked from and joined back into `s` (two branches of a captured graph).
+    // Their CTAs cannot share an SM (registers), so the per-pair CTAs take the SMs the
+    // factored launch's last CTAs leave, and neither launch ends with an idle tail.
+    const uint32_t n_pp = b->n_units - b->n_fact;
+    const bool fork = n_pp && b->n_fact;
+    if (fork) {
+        BPGB_CUDA_TRY(cudaEventRecord(b->ev_fork, s));
+        BPGB_CUDA_TRY(cudaStreamWaitEvent(b->side_stream, b->ev_fork, 0));
+    }
+    for (int f = 1; f >= 0; f--) {
         uint32_t nu = f ? b->n_fact : n_pp;
         if (!nu) continue;
+        const cudaStream_t ls = (fork && f == 0) ? b->side_stream : s;
         const BatchUnit *units = b->d_units + (f ? n_pp : 0);
         unsigned int *sched = b->d_sched + (f ? 2 : 0);
         void *kern = select_batch_kernel(b->dtype, b->checked, b->planar, f != 0);
@@ -2157,16 +2173,20 @@ int batch_execute(BatchPlan *b, const void *d_H, float *d_out, cudaStream_t s) {
                         (void *)&b->d_scratch, (void *)&b->d_diag,   (void *)&sched,
                         (void *)&b->ring[f].stages, (void *)&b->spin_limit};
         BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(f ? b->grid_fact : b->grid), dim3(288), args,
-                                       b->ring[f].smem, s));
+                                       b->ring[f].smem, ls));
         count_launches(1);
         for (const auto &sp : b->splits) {  // partial sums of this launch's split captures
             if (sp.fact != f) continue;
             const unsigned blocks = (unsigned)std::min<uint64_t>((sp.nvox + 255) / 256, 152ull * 8);
-            reduce_splits_kernel<false, false><<<blocks, 256, 0, s>>>(
+            reduce_splits_kernel<false, false><<<blocks, 256, 0, ls>>>(
                 b->d_scratch + sp.part_off, d_out + sp.out_off, sp.nvox, sp.splits, sp.scale);
             count_launches(1);
         }
         BPGB_CUDA_TRY(cudaGetLastError());
+    }
+    if (fork) {
+        BPGB_CUDA_TRY(cudaEventRecord(b->ev_join, b->side_stream));
+        BPGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     }
     b->last_stream = s;
     return BPGB_OK;
@@ -2449,6 +2469,9 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     if (e == cudaSuccess) e = cudaMalloc(&b->d_sched, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaMemset(b->d_sched, 0, 4 * sizeof(unsigned int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         batch_free(b);
         return cuda_error(e, "batch upload");
