@@ -34,7 +34,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 
-CU_SOURCES = ["bp_exact.cu", "bp_fast.cu", "phasor.cu", "geometry.cu", "diag.cu", "octree.cu", "cnn.cu", "rows.cu", "eval64.cu"]
+CU_SOURCES = ["bp_exact.cu", "bp_fast.cu", "phasor.cu", "geometry.cu", "diag.cu", "octree.cu", "cnn.cu", "cnn_tc.cu", "rows.cu", "eval64.cu"]
 CPP_SOURCES = ["capi.cpp", "capture.cpp", "shim.cpp", "synth.cpp", "tune.cpp", "npy.cpp",
                "octree_host.cpp"]
 

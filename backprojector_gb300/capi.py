@@ -132,6 +132,7 @@ SIGNATURES: dict[str, tuple] = {
                                     C.c_float, _P, _P]),
     "bpgb_plan_select_tiles_topk": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "bpgb_diag_mufu_rates": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
+    "bpgb_diag_umma_probe": (C.c_int, [_P, C.c_uint32, _U32, _F, _U32]),
     "bpgb_set_dropin_algo": (C.c_int, [C.c_int]),
     "bpgb_get_dropin_algo": (C.c_int, []),
     "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -214,6 +215,20 @@ SIGNATURES: dict[str, tuple] = {
                                 C.c_float, C.c_uint32, _P]),
     "bpgb_cnn_normalize": (C.c_int, [_P, _U32, C.c_uint32, _P, _P]),
     "bpgb_cnn_features": (C.c_int, [_P, _U32, C.c_uint32, _P, _P, _P]),
+    "bpgb_cnn_lp_bytes": (C.c_uint64, [C.c_uint32, C.c_uint32, _U32, C.c_uint32]),
+    "bpgb_cnn_tc_weight_bytes": (C.c_uint64, [C.c_uint32]),
+    "bpgb_cnn_lp_pack": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, C.c_uint32, _P,
+                                   _P]),
+    "bpgb_cnn_lp_unpack": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, _P]),
+    "bpgb_cnn_tc_pack_weights": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "bpgb_cnn_tc_conv3d": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, _P,
+                                     C.c_uint32, C.c_int, _P, _P, C.c_uint32, _P, _P]),
+    "bpgb_cnn_tc_wgrad_scratch_bytes": (C.c_uint64, [C.c_uint32, _U32, C.c_uint32]),
+    "bpgb_cnn_tc_conv3d_wgrad": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, _U32, C.c_uint32, _P,
+                                           C.c_uint64, _P, _P]),
+    "bpgb_cnn_tc_bce_grad": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_float, C.c_float, _P, _P,
+                                       _P]),
+    "bpgb_cnn_tc_status": (C.c_int, [_U32, C.c_int]),
 }
 
 _lib = None
@@ -290,6 +305,19 @@ def mufu_rates() -> dict:
     r = (C.c_double * 6)()
     check(lib().bpgb_diag_mufu_rates(r, 6), "bpgb_diag_mufu_rates")
     return dict(zip(("rsqrt_8_chains", "rsqrt_16_chains", "ex2", "sqrt", "rcp", "sin"), list(r)))
+
+
+def umma_probe(image: np.ndarray, params, ncols: int):
+    """Run bpgb_diag_umma_probe: image (<= 48 KB of bytes), params = (a_off, a_lbo, a_sbo,
+    a_kstep, b_off, b_lbo, b_sbo, b_kstep, idesc, nk); returns (accumulator [128, ncols]
+    FP32, status)."""
+    img = np.ascontiguousarray(image).view(np.uint8).reshape(-1)
+    prm = np.asarray(list(params) + [ncols], dtype=np.uint32)
+    out = np.empty((128, ncols), np.float32)
+    st = np.zeros(1, np.uint32)
+    check(lib().bpgb_diag_umma_probe(img.ctypes.data, img.nbytes, u32ptr(prm), fptr(out),
+                                     u32ptr(st)), "bpgb_diag_umma_probe")
+    return out, int(st[0])
 
 
 def launch_count() -> int:
@@ -737,6 +765,69 @@ def laplacian7(d_volume, voxels_per_side, d_out, stream=None) -> None:
 def cnn_features(d_coarse, dims, batch: int, d_X, d_scratch=None, stream=None) -> None:
     check(lib().bpgb_cnn_features(_ptr(d_coarse), u32ptr(_dims(dims)), int(batch), _ptr(d_X),
                                   _ptr(d_scratch), _stream_ptr(stream)), "bpgb_cnn_features")
+
+
+# ---- occupancy CNN on the tcgen05 tensor cores (line-planes tensors)
+
+def cnn_lp_bytes(channels: int, zpad: int, dims, batch: int) -> int:
+    return int(lib().bpgb_cnn_lp_bytes(int(channels), int(zpad), u32ptr(_dims(dims)), int(batch)))
+
+
+def cnn_tc_weight_bytes(in_channels: int) -> int:
+    return int(lib().bpgb_cnn_tc_weight_bytes(int(in_channels)))
+
+
+def cnn_lp_pack(d_X, channels: int, x_stride: int, dims, batch: int, zpad: int, d_lp,
+                stream=None) -> None:
+    check(lib().bpgb_cnn_lp_pack(_ptr(d_X), int(channels), int(x_stride), u32ptr(_dims(dims)),
+                                 int(batch), int(zpad), _ptr(d_lp), _stream_ptr(stream)),
+          "bpgb_cnn_lp_pack")
+
+
+def cnn_lp_unpack(d_lp, channels: int, zpad: int, dims, batch: int, d_X, stream=None) -> None:
+    check(lib().bpgb_cnn_lp_unpack(_ptr(d_lp), int(channels), int(zpad), u32ptr(_dims(dims)),
+                                   int(batch), _ptr(d_X), _stream_ptr(stream)), "bpgb_cnn_lp_unpack")
+
+
+def cnn_tc_pack_weights(d_W, cin: int, cout: int, d_Wf, d_Wb=None, stream=None) -> None:
+    check(lib().bpgb_cnn_tc_pack_weights(_ptr(d_W), int(cin), int(cout), _ptr(d_Wf), _ptr(d_Wb),
+                                         _stream_ptr(stream)), "bpgb_cnn_tc_pack_weights")
+
+
+def cnn_tc_conv3d(d_X, in_channels: int, in_zpad: int, dims, batch: int, d_W, d_bias,
+                  out_channels: int, relu: bool, d_mask=None, d_Y=None, out_zpad: int = 0,
+                  d_Yf=None, stream=None) -> None:
+    check(lib().bpgb_cnn_tc_conv3d(_ptr(d_X), int(in_channels), int(in_zpad), u32ptr(_dims(dims)),
+                                   int(batch), _ptr(d_W), _ptr(d_bias), int(out_channels),
+                                   1 if relu else 0, _ptr(d_mask), _ptr(d_Y), int(out_zpad),
+                                   _ptr(d_Yf), _stream_ptr(stream)), "bpgb_cnn_tc_conv3d")
+
+
+def cnn_tc_wgrad_scratch_bytes(in_channels: int, dims, batch: int) -> int:
+    return int(lib().bpgb_cnn_tc_wgrad_scratch_bytes(int(in_channels), u32ptr(_dims(dims)),
+                                                     int(batch)))
+
+
+def cnn_tc_conv3d_wgrad(d_X, in_channels: int, d_dY, out_channels: int, dims, batch: int,
+                        d_scratch, scratch_bytes: int, d_dW, stream=None) -> None:
+    check(lib().bpgb_cnn_tc_conv3d_wgrad(_ptr(d_X), int(in_channels), _ptr(d_dY),
+                                         int(out_channels), u32ptr(_dims(dims)), int(batch),
+                                         _ptr(d_scratch), int(scratch_bytes), _ptr(d_dW),
+                                         _stream_ptr(stream)), "bpgb_cnn_tc_conv3d_wgrad")
+
+
+def cnn_tc_bce_grad(d_logits, d_labels, dims, batch: int, pos_weight: float, scale: float, d_dZ,
+                    d_loss=None, stream=None) -> None:
+    check(lib().bpgb_cnn_tc_bce_grad(_ptr(d_logits), _ptr(d_labels), u32ptr(_dims(dims)),
+                                     int(batch), float(pos_weight), float(scale), _ptr(d_dZ),
+                                     _ptr(d_loss), _stream_ptr(stream)), "bpgb_cnn_tc_bce_grad")
+
+
+def cnn_tc_status(reset: bool = True) -> int:
+    """Synchronises; the tensor-core CNN kernels' timeout bits (0 = none)."""
+    st = np.zeros(1, np.uint32)
+    check(lib().bpgb_cnn_tc_status(u32ptr(st), 1 if reset else 0), "bpgb_cnn_tc_status")
+    return int(st[0])
 
 
 def rows_absmax(d_H, rows: int, T: int, pitch: int, d_max, stream=None) -> None:

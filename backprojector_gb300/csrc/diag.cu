@@ -12,6 +12,7 @@
 
 #include "bpgb_device.cuh"
 #include "bpgb_internal.h"
+#include "bpgb_umma.cuh"
 
 namespace bpgb {
 namespace {
@@ -141,10 +142,135 @@ double per_sm_rate(const std::vector<ProbeOut> &h, int sms, double ops_per_cta) 
     return used ? sum / used : 0.0;
 }
 
+// ---- tcgen05 known-answer probe ------------------------------------------------------
+// One CTA copies a 48 KB operand image into shared memory (the rest of its 96 KB zeroed),
+// issues `nk` tcgen05.mma kind::f16 (BF16, K = 16 each) with descriptors built from the
+// given offsets and strides, and dumps the 128 lanes x ncols FP32 columns of the
+// accumulator.  The host checks every stride combination against the 96 KB before the
+// launch, so any reading of the descriptors stays inside the CTA's shared memory.
+constexpr uint32_t kUmmaImage = 48 * 1024;
+constexpr uint32_t kUmmaSmem = 96 * 1024;
+constexpr uint32_t kUmmaCols = 256;
+
+struct UmmaProbeArgs {
+    uint32_t a_off, a_lbo, a_sbo, a_kstep;
+    uint32_t b_off, b_lbo, b_sbo, b_kstep;
+    uint32_t idesc, nk, ncols;
+};
+
+__global__ void __launch_bounds__(128) umma_probe_kernel(const uint4 *__restrict__ image,
+                                                         UmmaProbeArgs a, float *__restrict__ out,
+                                                         uint32_t *__restrict__ status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t taddr_s;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint4 *s4 = reinterpret_cast<uint4 *>(smem);
+    for (uint32_t i = tid; i < kUmmaSmem / 16; i += 128)
+        s4[i] = i < kUmmaImage / 16 ? image[i] : make_uint4(0, 0, 0, 0);
+    if (warp == 0) {
+        tmem_alloc(smem_addr(&taddr_s), kUmmaCols);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(smem_addr(&bar), 1);
+        mbar_fence_init();
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = taddr_s;
+    if (tid == 0) {
+        const uint32_t base = smem_addr(smem);
+        for (uint32_t k = 0; k < a.nk; k++)
+            umma_bf16(taddr, umma_smem_desc(base + a.a_off + k * a.a_kstep, a.a_lbo, a.a_sbo),
+                      umma_smem_desc(base + a.b_off + k * a.b_kstep, a.b_lbo, a.b_sbo), a.idesc,
+                      k > 0);
+        umma_commit(smem_addr(&bar));
+    }
+    bool done = mbar_wait(smem_addr(&bar), 0, 1u << 24);
+    tc_fence_after();
+    if (done) {
+        for (uint32_t c = 0; c < a.ncols; c += 16) {
+            float v[16];
+            tmem_ld16(taddr + ((warp * 32u) << 16) + c, v);
+            tmem_ld_wait();
+            float *o = out + (uint64_t)(warp * 32 + lane) * a.ncols + c;
+#pragma unroll
+            for (int j = 0; j < 16; j++) o[j] = v[j];
+        }
+    } else {
+        if (lane == 0) atomicOr(status, 1u);
+        // the MMAs may still read shared memory and write the accumulator: wait (bounded)
+        // before the columns are released
+        done = mbar_wait(smem_addr(&bar), 0, 1u << 26);
+        if (!done && lane == 0) atomicOr(status, 2u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(taddr, kUmmaCols);
+    }
+}
+
 }  // namespace
 }  // namespace bpgb
 
 using namespace bpgb;
+
+// params: a_off, a_lbo, a_sbo, a_kstep, b_off, b_lbo, b_sbo, b_kstep, idesc, nk, ncols.
+extern "C" int bpgb_diag_umma_probe(const void *h_image, uint32_t image_bytes,
+                                    const uint32_t *params, float *h_out, uint32_t *h_status) {
+    clear_error();
+    if (!h_image || !params || !h_out || !h_status || image_bytes > kUmmaImage ||
+        image_bytes % 16)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad umma probe arguments");
+    UmmaProbeArgs a{params[0], params[1], params[2], params[3], params[4], params[5],
+                    params[6], params[7], params[8], params[9], params[10]};
+    if (a.nk == 0 || a.nk > 8 || a.ncols == 0 || a.ncols > kUmmaCols || a.ncols % 16)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "umma probe: nk in 1..8, ncols in 16..256");
+    // whichever stride the hardware applies along either dimension, at most 32 core
+    // matrices (256 rows) are stepped along M/N and 2 along K per MMA
+    const uint64_t far_a = (uint64_t)a.a_off + (uint64_t)(a.nk - 1) * a.a_kstep +
+                           32ull * (a.a_lbo + a.a_sbo) + 128;
+    const uint64_t far_b = (uint64_t)a.b_off + (uint64_t)(a.nk - 1) * a.b_kstep +
+                           32ull * (a.b_lbo + a.b_sbo) + 128;
+    if (far_a > kUmmaSmem || far_b > kUmmaSmem || a.a_off % 16 || a.b_off % 16 ||
+        a.a_lbo % 16 || a.a_sbo % 16 || a.b_lbo % 16 || a.b_sbo % 16 || a.a_kstep % 16 ||
+        a.b_kstep % 16)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT,
+                         "umma probe: operand extents must stay inside 96 KB, 16-byte units");
+    int st = require_device();
+    if (st) return st;
+    uint4 *d_img = nullptr;
+    float *d_out = nullptr;
+    uint32_t *d_st = nullptr;
+    const size_t out_bytes = (size_t)128 * a.ncols * sizeof(float);
+    cudaError_t e = cudaMalloc(&d_img, kUmmaImage);
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, out_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&d_st, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(d_img, 0, kUmmaImage);
+    if (e == cudaSuccess) e = cudaMemcpy(d_img, h_image, image_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(d_out, 0xFF, out_bytes);
+    if (e == cudaSuccess) e = cudaMemset(d_st, 0, sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(umma_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kUmmaSmem);
+    if (e == cudaSuccess) {
+        umma_probe_kernel<<<1, 128, kUmmaSmem>>>(d_img, a, d_out, d_st);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h_out, d_out, out_bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(h_status, d_st, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_img);
+    cudaFree(d_out);
+    cudaFree(d_st);
+    if (e != cudaSuccess) return cuda_error(e, "umma probe");
+    return BPGB_OK;
+}
 
 extern "C" int bpgb_diag_mufu_rates(double *rates, int n) {
     clear_error();

@@ -409,6 +409,51 @@ int bpgb_cnn_normalize(const float *d_coarse, const uint32_t *dims, uint32_t bat
 int bpgb_cnn_features(const float *d_coarse, const uint32_t *dims, uint32_t batch, void *d_X,
                       float *d_scratch, void *stream);
 
+/* ---- occupancy CNN on the tcgen05 tensor cores (the training step) ------------------
+ * Line-planes tensors: volumes of dims = {n0, n1, 32} (n1 a multiple of 8) per sample,
+ * rows of 16 bytes holding 8 BF16 channels (1 plane for <= 8 channels, 2 for <= 16),
+ *   row(s, x', y', h, z') = (((s (n0+2) + x') (n1+2) + y') planes + h) (32 + 2 zpad) + z'
+ * with x' = x + 1, y' = y + 1, z' = z + zpad, and zero lines after the last sample.  The
+ * caller allocates bpgb_cnn_lp_bytes and clears the buffer once: padding rows must stay
+ * zero, and the kernels write interior rows only.  Forward inputs (activations) use
+ * zpad = 0, backward inputs (gradients) zpad = 1.  Weights are the FP32 masters [KP][COUT]
+ * of bpgb_cnn_conv3d (row t cin + ci, bias row 27 cin), packed per call site into
+ * tensor-core images of bpgb_cnn_tc_weight_bytes(input channels). */
+uint64_t bpgb_cnn_lp_bytes(uint32_t channels, uint32_t zpad, const uint32_t *dims,
+                           uint32_t batch);
+uint64_t bpgb_cnn_tc_weight_bytes(uint32_t in_channels);
+/* Interior rows from / to channels-last BF16 [V][x_stride] (V = batch n0 n1 32). */
+int bpgb_cnn_lp_pack(const void *d_X, uint32_t channels, uint32_t x_stride, const uint32_t *dims,
+                     uint32_t batch, uint32_t zpad, void *d_lp, void *stream);
+int bpgb_cnn_lp_unpack(const void *d_lp, uint32_t channels, uint32_t zpad, const uint32_t *dims,
+                       uint32_t batch, void *d_X, void *stream);
+/* Forward image (cin inputs) into d_Wf; backward-data image (cout inputs, taps flipped,
+ * channels transposed) into d_Wb when non-null. */
+int bpgb_cnn_tc_pack_weights(const float *d_W, uint32_t cin, uint32_t cout, void *d_Wf,
+                             void *d_Wb, void *stream);
+/* 3x3x3 convolution, zero padding: Y = act(conv(X) + bias) on the tensor cores.  d_bias
+ * (out_channels FP32, or null), relu, d_mask (an activation-layout tensor of out_channels:
+ * outputs where mask <= 0 are zeroed -- the ReLU derivative of the backward pass), d_Y
+ * (out_channels, out_zpad) and/or d_Yf (channel 0 as FP32 [V]). */
+int bpgb_cnn_tc_conv3d(const void *d_X, uint32_t in_channels, uint32_t in_zpad,
+                       const uint32_t *dims, uint32_t batch, const void *d_W, const float *d_bias,
+                       uint32_t out_channels, int relu, const void *d_mask, void *d_Y,
+                       uint32_t out_zpad, float *d_Yf, void *stream);
+/* dW [bpgb_cnn_kp(in_channels)][out_channels] (FP32, bias row 27 in_channels, padding rows
+ * zero) of activation d_X (zpad 0) and output gradient d_dY (zpad 1). */
+uint64_t bpgb_cnn_tc_wgrad_scratch_bytes(uint32_t in_channels, const uint32_t *dims,
+                                         uint32_t batch);
+int bpgb_cnn_tc_conv3d_wgrad(const void *d_X, uint32_t in_channels, const void *d_dY,
+                             uint32_t out_channels, const uint32_t *dims, uint32_t batch,
+                             float *d_scratch, uint64_t scratch_bytes, float *d_dW, void *stream);
+/* bpgb_cnn_bce_grad writing dZ as a single-plane gradient (zpad 1); logits and labels [V]. */
+int bpgb_cnn_tc_bce_grad(const float *d_logits, const uint8_t *d_labels, const uint32_t *dims,
+                         uint32_t batch, float pos_weight, float scale, void *d_dZ, float *d_loss,
+                         void *stream);
+/* Synchronises the device and reads the tensor-core kernels' timeout bits (0 = none);
+ * clears them when reset != 0. */
+int bpgb_cnn_tc_status(uint32_t *status, int reset);
+
 /* ---- learned octree as one native object --------------------------------------------
  * Replaces the reference's octree entry (call_cuda_octree_backprojection,
  * backproject_cuda.hpp:30-39, whose GPU implementation backproject_cuda.cu:503-669 prints
@@ -496,6 +541,17 @@ int bpgb_diag_pipe_rates(double *rates);
  * [5] sin.approx (the first n of them).  For the roofline of the FAST kernel, whose
  * update costs one rsqrt. */
 int bpgb_diag_mufu_rates(double *rates, int n);
+
+/* Known-answer probe of the tensor-core path (tcgen05.mma kind::f16, BF16 operands, FP32
+ * accumulate): one CTA copies the 48 KB host image `h_image` into shared memory, issues
+ * params[9] MMAs (K = 16 each) whose descriptors are built from params = {a_off, a_lbo,
+ * a_sbo, a_kstep, b_off, b_lbo, b_sbo, b_kstep, idesc, nk, ncols} (byte offsets into the
+ * image; MMA k adds k * kstep to the start), and writes the accumulator's 128 lanes x
+ * ncols FP32 columns to h_out (row-major).  Every stride combination is checked to stay
+ * inside the CTA's 96 KB of shared memory before the launch.  *h_status: bit 0 = the
+ * commit wait ran out.  Pins the descriptor and accumulator layouts the CNN kernels use. */
+int bpgb_diag_umma_probe(const void *h_image, uint32_t image_bytes, const uint32_t *params,
+                         float *h_out, uint32_t *h_status);
 
 /* ---- phasor pulse --------------------------------------------------------
  * d_out[r, t] = sum_k d_H[r, t + k - K/2] * (cos_k, sin_k), read index in (0, T), with
