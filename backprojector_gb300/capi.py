@@ -221,6 +221,9 @@ SIGNATURES: dict[str, tuple] = {
                                    _P]),
     "bpgb_cnn_lp_unpack": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, _P]),
     "bpgb_cnn_tc_pack_weights": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "bpgb_cnn_tc_pack_layers": (C.c_int, [C.POINTER(C.c_void_p), _U32, _U32,
+                                          C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                          C.c_uint32, _P]),
     "bpgb_cnn_tc_conv3d": (C.c_int, [_P, C.c_uint32, C.c_uint32, _U32, C.c_uint32, _P, _P,
                                      C.c_uint32, C.c_int, _P, _P, C.c_uint32, _P, _P]),
     "bpgb_cnn_tc_wgrad_scratch_bytes": (C.c_uint64, [C.c_uint32, _U32, C.c_uint32]),
@@ -792,6 +795,18 @@ def cnn_lp_unpack(d_lp, channels: int, zpad: int, dims, batch: int, d_X, stream=
 def cnn_tc_pack_weights(d_W, cin: int, cout: int, d_Wf, d_Wb=None, stream=None) -> None:
     check(lib().bpgb_cnn_tc_pack_weights(_ptr(d_W), int(cin), int(cout), _ptr(d_Wf), _ptr(d_Wb),
                                          _stream_ptr(stream)), "bpgb_cnn_tc_pack_weights")
+
+
+def cnn_tc_pack_layers(d_Ws, cins, couts, d_Wfs, d_Wbs, stream=None) -> None:
+    """bpgb_cnn_tc_pack_layers: lists of masters, channel counts, images (None allowed in d_Wbs)."""
+    L = len(d_Ws)
+    W = (C.c_void_p * L)(*[_ptr(w) for w in d_Ws])
+    F = (C.c_void_p * L)(*[_ptr(w) for w in d_Wfs])
+    B = (C.c_void_p * L)(*[_ptr(w) if w is not None else None for w in d_Wbs])
+    ci = np.asarray(cins, np.uint32)
+    co = np.asarray(couts, np.uint32)
+    check(lib().bpgb_cnn_tc_pack_layers(W, u32ptr(ci), u32ptr(co), F, B, L, _stream_ptr(stream)),
+          "bpgb_cnn_tc_pack_layers")
 
 
 def cnn_tc_conv3d(d_X, in_channels: int, in_zpad: int, dims, batch: int, d_W, d_bias,

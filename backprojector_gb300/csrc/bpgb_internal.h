@@ -1,6 +1,7 @@
 // Internal declarations shared by the host-side translation units of libbpgb300.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -26,6 +27,15 @@ void count_launches(uint64_t n);
 
 // Checks that a GB300-class device (compute capability 10.x) is current.
 int require_device(int *sm_count = nullptr);
+
+// cuTensorMapEncodeTiled from the driver (looked up once, no libcuda link needed), or
+// null when the driver does not provide it.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                   CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder();
 
 // Raises (never lowers) a kernel's dynamic shared memory limit on the current device to
 // at least `bytes`.  Plans and batches that share a kernel function stay launchable

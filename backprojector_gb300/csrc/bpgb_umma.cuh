@@ -1,16 +1,17 @@
 // tcgen05 (5th-generation tensor core) helpers for sm_103a: tensor-memory allocation,
 // shared-memory matrix descriptors, instruction descriptors for kind::f16 (BF16 operands,
-// FP32 accumulate), MMA issue, commit to an mbarrier, tensor-memory loads, and the untiled
-// bulk copy global -> shared that stages the operands.
+// FP32 accumulate), MMA issue, commit to an mbarrier, tensor-memory loads, and the bulk
+// and tiled (TMA) copies global -> shared that stage the operands.
 //
 // Descriptor formats follow the PTX ISA's tcgen05 chapter (shared-memory descriptor and
 // instruction descriptor tables).  Operands here are always in the no-swizzle canonical
 // layout: a "core matrix" is 8 rows of 16 bytes stored contiguously (128 B).  For a
 // K-major operand a row is one M (or N) index holding 8 consecutive K elements; for an
 // MN-major operand a row is one K index holding 8 consecutive M (or N) elements.  The two
-// strides of the descriptor place the core matrices: one between neighbours along K and
-// one between neighbours along M/N (which field carries which is pinned by the known-answer
-// test of bpgb_diag_umma_probe and recorded in kUmma* below).
+// strides of the descriptor place the core matrices: the leading byte offset (LBO) is the
+// stride between neighbours along K and the stride byte offset (SBO) the one along M/N,
+// for K-major and MN-major operands alike (pinned by the known-answer test of
+// bpgb_diag_umma_probe).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -119,6 +120,28 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
         ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+// 4-D tiled TMA load of one box at coordinates (c0 innermost .. c3) into shared memory,
+// completing on bar.  c0 x element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void *map, int32_t c0, int32_t c1,
+                                            int32_t c2, int32_t c3, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+
+// 5-D tiled TMA load of one box at coordinates (c0 innermost .. c4) into shared memory,
+// completing on bar.  c0 x element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const void *map, int32_t c0, int32_t c1,
+                                            int32_t c2, int32_t c3, int32_t c4, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
         : "memory");
 }
 

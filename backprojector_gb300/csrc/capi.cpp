@@ -55,6 +55,20 @@ int require_device(int *sm_count) {
     return BPGB_OK;
 }
 
+EncodeTiledFn tensor_map_encoder() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
 int reserve_dynamic_smem(const void *kernel, uint32_t bytes) {
     static std::mutex mu;
     static std::map<std::pair<int, const void *>, uint32_t> limits;

@@ -76,8 +76,6 @@ struct Lp {
 
 __device__ __forceinline__ void fail(uint32_t bit) { atomicOr(&g_tc_status, bit); }
 
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
-
 __device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
     const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t *>(&p);
@@ -87,38 +85,38 @@ __device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w <<
 __device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
 // ---- convolution --------------------------------------------------------------------
-constexpr uint32_t kConvLB = 4;                // output lines per block (same s, x)
-constexpr uint32_t kConvSlabLines = kConvLB + 3;  // y' lines staged per x' (last one spare)
+constexpr uint32_t kConvLB = 4;                       // output lines per block (M = 128)
+constexpr uint32_t kConvLines = kConvLB + 3;          // y' lines staged per (x', plane), 1 spare
+constexpr uint32_t kConvBox = kConvLines * 32 * 16;   // bytes of one staged (x', plane) box
+constexpr uint32_t kConvStages = 4;
+constexpr uint32_t kConvAhead = 2;                    // a stage is refilled 2 blocks after use
 constexpr uint32_t kConvThreads = 160;
-constexpr uint32_t kConvCols = 2 * kConvLB * 32;  // two accumulator buffers
-constexpr uint32_t kEStride = 33;                 // floats per (dz, co) row of the exchange
+constexpr uint32_t kConvN = 48;                       // dz x 16 output channels
+constexpr uint32_t kConvAccs = 4;                     // accumulators in flight
+constexpr uint32_t kConvAcc = 64;                     // columns per accumulator
+constexpr uint32_t kConvCols = kConvAccs * kConvAcc;  // 256: two CTAs per SM
+constexpr uint32_t kConvGroup = kConvN * 16 * 2;      // one K = 16 weight group: 1536 B
 
 struct ConvArgs {
-    const uint8_t *X;
     Lp in;
-    const uint8_t *W;  // weight image: groups x 2 KB
-    const float *bias;  // cout values or null
+    const uint8_t *W;    // weight image: groups x 1536 B
+    const float *bias;   // cout values or null
     uint32_t cout;
     int relu;
-    const uint8_t *mask;  // activation-layout tensor of the output's channels, or null
+    const uint8_t *mask; // activation-layout tensor of the output's channels, or null
     Lp mk;
-    uint8_t *Y;  // output tensor or null
+    uint8_t *Y;          // output tensor or null
     Lp out;
-    float *Yf;  // channel 0 in FP32 [batch n0 n1 32], or null
+    float *Yf;           // channel 0 in FP32 [batch n0 n1 32], or null
     uint32_t nblocks;
 };
 
 template <int NPL>
 struct ConvShape {
     static constexpr uint32_t kGroups = NPL == 2 ? 9 : 5;
-    static constexpr uint32_t kWBytes = kGroups * 2048;
-    static __host__ __device__ uint32_t line_bytes(uint32_t zp) { return NPL * (kZLine + 2 * zp) * 16; }
-    static __host__ __device__ uint32_t slabx(uint32_t zp) { return kConvSlabLines * line_bytes(zp); }
-    static __host__ __device__ uint32_t slab(uint32_t zp) { return 3 * slabx(zp); }
-    static constexpr uint32_t kEBytes = kConvLB * 3 * 16 * kEStride * 4;
-    static __host__ __device__ uint32_t smem(uint32_t zp) {
-        return kWBytes + 2 * slab(zp) + kEBytes;
-    }
+    static constexpr uint32_t kWBytes = kGroups * kConvGroup;
+    static constexpr uint32_t kStage = 3 * NPL * kConvBox;
+    static constexpr uint32_t kSmem = kWBytes + kConvStages * kStage;
 };
 
 __device__ __forceinline__ void conv_block(uint32_t b, const Lp &in, uint32_t &s, uint32_t &x,
@@ -131,27 +129,35 @@ __device__ __forceinline__ void conv_block(uint32_t b, const Lp &in, uint32_t &s
     y0 = (r - x * per_x) * kConvLB;
 }
 
+// One block = 4 consecutive output lines (y0 .. y0 + 3) of one (sample, x): M = 128 voxels
+// (row 32 j + z = line j, voxel z), N = 48 = (dz, co), K = 16.  The stage holds, for each
+// dx and plane h, the box of lines y' = y0 .. y0 + 6 without z-padding ([line][z][8 ch]),
+// so tap (dx, dy) is the A operand at box(dx, plane 0) + dy x 512 B (core matrices of 8
+// voxels at 128 B, the second plane at +kConvBox); single-plane inputs pair two taps as
+// the two K groups.  Accumulator row = TMEM lane, so warp j's lane z holds voxel z of line
+// j: the dz recombination is a shuffle up / down within the warp.
 template <int NPL>
-__global__ void __launch_bounds__(kConvThreads) conv_tc_kernel(ConvArgs a) {
+__global__ void __launch_bounds__(kConvThreads)
+    conv_tc_kernel(const __grid_constant__ CUtensorMap tmap, ConvArgs a) {
     using S = ConvShape<NPL>;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t full[2], empty[2], acc_full[2], acc_empty[2], drain;
+    __shared__ __align__(8) uint64_t full[kConvStages], empty[kConvStages], acc_full[kConvAccs],
+        acc_empty[kConvAccs], drain;
     __shared__ uint32_t taddr_s;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t zp = a.in.zp;
-    const uint32_t line_bytes = S::line_bytes(zp), slabx = S::slabx(zp), slab_bytes = S::slab(zp);
     uint8_t *w_s = smem;
-    uint8_t *slab_s = smem + S::kWBytes;
-    float *E = reinterpret_cast<float *>(slab_s + 2 * slab_bytes);
+    uint8_t *stage_s = smem + S::kWBytes;
 
     if (warp == 0) {
         tmem_alloc(smem_addr(&taddr_s), kConvCols);
         tmem_relinquish();
     }
     if (tid == 128) {
-        for (int i = 0; i < 2; i++) {
+        for (uint32_t i = 0; i < kConvStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
             mbar_init(smem_addr(&empty[i]), 1);
+        }
+        for (uint32_t i = 0; i < kConvAccs; i++) {
             mbar_init(smem_addr(&acc_full[i]), 1);
             mbar_init(smem_addr(&acc_empty[i]), 128);
         }
@@ -164,141 +170,140 @@ __global__ void __launch_bounds__(kConvThreads) conv_tc_kernel(ConvArgs a) {
     const uint32_t taddr = taddr_s;
 
     if (tid == 128) {
-        // ---- producer and MMA issue
-        auto copy = [&](uint32_t buf, uint32_t b, bool weights) {
+        // ---- producer (TMA) and MMA issue, one thread.  Stage of local block i:
+        // i % kConvStages; the
+        // stage of block it - kConvAhead (whose MMAs completed long ago) is refilled with
+        // block it - kConvAhead + kConvStages right after block it's MMAs are issued.
+        auto copy = [&](uint32_t st, uint32_t b, bool weights) {
             uint32_t s, x, y0;
             conv_block(b, a.in, s, x, y0);
-            const uint32_t bar = smem_addr(&full[buf]);
-            mbar_expect_tx(bar, slab_bytes + (weights ? S::kWBytes : 0u));
+            const uint32_t bar = smem_addr(&full[st]);
+            mbar_expect_tx(bar, S::kStage + (weights ? S::kWBytes : 0u));
             if (weights) bulk_g2s(smem_addr(w_s), a.W, S::kWBytes, bar);
-            const uint32_t dst = smem_addr(slab_s + buf * slab_bytes);
+            const uint32_t dst = smem_addr(stage_s + st * S::kStage);
+            const int32_t xg = (int32_t)(s * (a.in.n0 + 2) + x);
             for (uint32_t dx = 0; dx < 3; dx++)
-                bulk_g2s(dst + dx * slabx, a.X + a.in.row(s, x + dx, y0, 0, 0) * 16, slabx, bar);
+                for (uint32_t h = 0; h < NPL; h++)
+                    tma_load_4d(dst + (dx * NPL + h) * kConvBox, &tmap, (int32_t)(a.in.zp * 8),
+                                (int32_t)h, (int32_t)y0, xg + (int32_t)dx, bar);
             mbar_arrive(bar);
         };
-        const uint32_t idesc = umma_idesc_bf16(64, 32, false, false);
+        const uint32_t idesc = umma_idesc_bf16(128, kConvN, false, false);
         const uint32_t wbase = smem_addr(w_s);
+        for (uint32_t i = 0; i < kConvStages; i++) {
+            const uint64_t b = blockIdx.x + (uint64_t)i * gridDim.x;
+            if (b >= a.nblocks) break;
+            copy(i, (uint32_t)b, i == 0);
+        }
         uint32_t it = 0;
-        if (blockIdx.x < a.nblocks) copy(0, blockIdx.x, true);
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
-            const uint32_t buf = it & 1, use = it >> 1;
-            if (!mbar_wait(smem_addr(&full[buf]), use & 1, kSpin)) {
+            const uint32_t st = it % kConvStages, ab = it % kConvAccs;
+            if (!mbar_wait(smem_addr(&full[st]), (it / kConvStages) & 1, kSpin)) {
                 fail(1);
                 break;
             }
-            if (use > 0 && !mbar_wait(smem_addr(&acc_empty[buf]), (use - 1) & 1, kSpin)) {
+            if (it >= kConvAccs &&
+                !mbar_wait(smem_addr(&acc_empty[ab]), ((it / kConvAccs) - 1) & 1, kSpin)) {
                 fail(2);
                 break;
             }
             tc_fence_after();
-            const uint32_t sb = smem_addr(slab_s + buf * slab_bytes) + zp * 16;
-            for (uint32_t j = 0; j < kConvLB; j++) {
-                const uint32_t d = taddr + buf * (kConvLB * 32) + j * 32;
-                for (uint32_t g = 0; g < S::kGroups; g++) {
-                    uint32_t b0, lbo;
-                    if (NPL == 2) {
-                        b0 = sb + (g / 3) * slabx + (j + g % 3) * line_bytes;
-                        lbo = (kZLine + 2 * zp) * 16;  // plane 1 of the same line
-                    } else {
-                        const uint32_t ta = 2 * g, tb = 2 * g + 1;
-                        b0 = sb + (ta / 3) * slabx + (j + ta % 3) * line_bytes;
-                        // second K group: the next tap (the tenth is a zero-weight slot that
-                        // reads the rows one voxel further on)
-                        lbo = tb < 9 ? sb + (tb / 3) * slabx + (j + tb % 3) * line_bytes - b0 : 16u;
-                    }
-                    umma_bf16(d, umma_smem_desc(wbase + g * 2048, 1024, 128),
-                              umma_smem_desc(b0, lbo, 128), idesc, g > 0);
+            const uint32_t base = smem_addr(stage_s + st * S::kStage);
+            const uint32_t d = taddr + ab * kConvAcc;
+#pragma unroll
+            for (uint32_t g = 0; g < S::kGroups; g++) {
+                uint32_t a0, lbo;
+                if (NPL == 2) {
+                    a0 = base + (g / 3) * 2 * kConvBox + (g % 3) * 512;
+                    lbo = kConvBox;  // plane 1 of the same lines
+                } else {
+                    const uint32_t ta = 2 * g, tb = 2 * g + 1;
+                    a0 = base + (ta / 3) * kConvBox + (ta % 3) * 512;
+                    // second K group: the next tap (the tenth is a zero-weight slot that
+                    // reads the rows one voxel further on)
+                    lbo = tb < 9 ? base + (tb / 3) * kConvBox + (tb % 3) * 512 - a0 : 16u;
                 }
+                umma_bf16(d, umma_smem_desc(a0, lbo, 128),
+                          umma_smem_desc(wbase + g * kConvGroup, kConvN * 16, 128), idesc, g > 0);
             }
-            umma_commit(smem_addr(&empty[buf]));
-            umma_commit(smem_addr(&acc_full[buf]));
-            const uint32_t nb = b + gridDim.x;
-            if (nb < a.nblocks) {
-                const uint32_t nbuf = (it + 1) & 1, nuse = (it + 1) >> 1;
-                if (nuse > 0 && !mbar_wait(smem_addr(&empty[nbuf]), (nuse - 1) & 1, kSpin)) {
-                    fail(4);
-                    break;
+            umma_commit(smem_addr(&empty[st]));
+            umma_commit(smem_addr(&acc_full[ab]));
+            if (it >= kConvAhead) {
+                const uint32_t old = it - kConvAhead;
+                const uint64_t pb = blockIdx.x + (uint64_t)(old + kConvStages) * gridDim.x;
+                if (pb < a.nblocks) {
+                    const uint32_t ps = old % kConvStages;
+                    if (!mbar_wait(smem_addr(&empty[ps]), (old / kConvStages) & 1, kSpin)) {
+                        fail(4);
+                        break;
+                    }
+                    copy(ps, (uint32_t)pb, false);
                 }
-                copy(nbuf, nb, false);
             }
         }
         umma_commit(smem_addr(&drain));
         if (!mbar_wait(smem_addr(&drain), 0, kSpin)) fail(8);
     } else if (tid < 128) {
-        // ---- epilogue: tensor memory -> z recombination -> bias / ReLU / mask -> BF16 rows
+        // ---- epilogue: one voxel per thread (warp = line, lane = z)
         uint32_t it = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
-            const uint32_t buf = it & 1, use = it >> 1;
-            if (!mbar_wait(smem_addr(&acc_full[buf]), use & 1, kSpin)) {
+            const uint32_t ab = it % kConvAccs;
+            if (!mbar_wait(smem_addr(&acc_full[ab]), (it / kConvAccs) & 1, kSpin)) {
                 fail(16);
                 break;
             }
             tc_fence_after();
+            float dm[16], d0[16], dp[16];
+            const uint32_t t = taddr + ((warp * 32u) << 16) + ab * kConvAcc;
+            tmem_ld16(t, dm);
+            tmem_ld16(t + 16, d0);
+            tmem_ld16(t + 32, dp);
+            tmem_ld_wait();
+            tc_fence_before();
+            mbar_arrive(smem_addr(&acc_empty[ab]));
             uint32_t s, x, y0;
             conv_block(b, a.in, s, x, y0);
-            if (warp < 3) {
-                for (uint32_t j = 0; j < kConvLB; j++) {
-                    float v[32];
-                    __syncwarp();
-                    const uint32_t t = taddr + ((warp * 32u) << 16) + buf * (kConvLB * 32) + j * 32;
-                    tmem_ld16(t, *reinterpret_cast<float(*)[16]>(&v[0]));
-                    tmem_ld16(t + 16, *reinterpret_cast<float(*)[16]>(&v[16]));
-                    tmem_ld_wait();
-                    if (lane < 16) {
-                        float *e = E + ((j * 3 + warp) * 16 + lane) * kEStride;
+            const uint32_t y = y0 + warp, z = lane;
+            float o[16];
 #pragma unroll
-                        for (int z = 0; z < 32; z++) e[z] = v[z];
-                    }
-                }
+            for (int co = 0; co < 16; co++) {
+                float up = __shfl_up_sync(0xffffffffu, dm[co], 1);
+                float dn = __shfl_down_sync(0xffffffffu, dp[co], 1);
+                if (lane == 0) up = 0.0f;
+                if (lane == 31) dn = 0.0f;
+                o[co] = (up + d0[co]) + dn;
             }
-            tc_fence_before();
-            mbar_arrive(smem_addr(&acc_empty[buf]));
-            epi_sync();
+            if (a.Yf)
+                a.Yf[(((uint64_t)s * a.in.n0 + x) * a.in.n1 + y) * 32 + z] =
+                    a.bias && a.cout > 0 ? o[0] + a.bias[0] : o[0];
             if (a.Y) {
-                const uint32_t chunks = kConvLB * 32 * a.out.npl;
-                for (uint32_t c = tid; c < chunks; c += 128) {
-                    const uint32_t h = c % a.out.npl, z = (c / a.out.npl) % 32,
-                                   j = c / (a.out.npl * 32);
-                    const float *e = E + (j * 3 * 16 + h * 8) * kEStride;
-                    float o[8];
 #pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const uint32_t co = h * 8 + k;
-                        const float *r = e + k * kEStride;
-                        float y = r[16 * kEStride + z];
-                        if (z > 0) y = r[z - 1] + y;
-                        if (z < 31) y = y + r[32 * kEStride + z + 1];
-                        if (a.bias && co < a.cout) y += a.bias[co];
-                        if (co >= a.cout) y = 0.0f;
-                        if (a.relu) y = fmaxf(y, 0.0f);
-                        o[k] = y;
-                    }
+                for (int co = 0; co < 16; co++) {
+                    float v = o[co];
+                    if (a.bias && (uint32_t)co < a.cout) v += a.bias[co];
+                    if ((uint32_t)co >= a.cout) v = 0.0f;
+                    if (a.relu) v = fmaxf(v, 0.0f);
+                    o[co] = v;
+                }
+#pragma unroll
+                for (uint32_t h = 0; h < 2; h++) {
+                    if (h >= a.out.npl) break;
+                    float *oh = o + 8 * h;
                     if (a.mask) {
                         const uint4 m = *reinterpret_cast<const uint4 *>(
-                            a.mask + a.mk.row(s, x + 1, y0 + j + 1, h, z + a.mk.zp) * 16);
+                            a.mask + a.mk.row(s, x + 1, y + 1, h, z + a.mk.zp) * 16);
                         const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
-                            if (!(bf_lo(mw[k]) > 0.0f)) o[2 * k] = 0.0f;
-                            if (!(bf_hi(mw[k]) > 0.0f)) o[2 * k + 1] = 0.0f;
+                            if (!(bf_lo(mw[k]) > 0.0f)) oh[2 * k] = 0.0f;
+                            if (!(bf_hi(mw[k]) > 0.0f)) oh[2 * k + 1] = 0.0f;
                         }
                     }
-                    *reinterpret_cast<uint4 *>(a.Y +
-                                               a.out.row(s, x + 1, y0 + j + 1, h, z + a.out.zp) * 16) =
-                        make_uint4(pack_bf2(o[0], o[1]), pack_bf2(o[2], o[3]), pack_bf2(o[4], o[5]),
-                                   pack_bf2(o[6], o[7]));
+                    *reinterpret_cast<uint4 *>(a.Y + a.out.row(s, x + 1, y + 1, h, z + a.out.zp) * 16) =
+                        make_uint4(pack_bf2(oh[0], oh[1]), pack_bf2(oh[2], oh[3]),
+                                   pack_bf2(oh[4], oh[5]), pack_bf2(oh[6], oh[7]));
                 }
             }
-            if (a.Yf) {
-                const uint32_t j = tid / 32, z = tid % 32;  // 128 threads = 4 lines x 32
-                const float *r = E + (j * 3 * 16) * kEStride;
-                float y = r[16 * kEStride + z];
-                if (z > 0) y = r[z - 1] + y;
-                if (z < 31) y = y + r[32 * kEStride + z + 1];
-                if (a.bias && a.cout > 0) y += a.bias[0];
-                a.Yf[(((uint64_t)s * a.in.n0 + x) * a.in.n1 + y0 + j) * 32 + z] = y;
-            }
-            epi_sync();
         }
     }
     tc_fence_before();
@@ -310,34 +315,33 @@ __global__ void __launch_bounds__(kConvThreads) conv_tc_kernel(ConvArgs a) {
 }
 
 // ---- weight gradient ----------------------------------------------------------------
-constexpr uint32_t kWgLB = 8;  // output lines per block
+constexpr uint32_t kWgLB = 4;       // output lines per block
+constexpr uint32_t kWgStages = 3;
 constexpr uint32_t kWgThreads = 160;
-constexpr uint32_t kWgCols = 256;  // 10 accumulators x 16 columns, rounded up
+constexpr uint32_t kWgCols = 128;   // M = 128 and M = 64 accumulators (48 columns) + bias (16)
+constexpr uint32_t kWgAcc64 = 48;   // column of the M = 64 accumulator
+constexpr uint32_t kWgBias = 96;    // column of the bias accumulator
 constexpr uint32_t kOnesBytes = 2048;
+constexpr uint32_t kWgBLine = 3 * 2 * 512;  // per output line: (k, plane) blocks of 32 rows
 
 struct WgradArgs {
-    const uint8_t *X;  // activation (zp 0)
-    Lp xin;
-    const uint8_t *dY;  // gradient (zp 1)
-    Lp dy;
+    Lp xin;            // activation (zp 0), read through its tensor map
+    Lp dy;             // gradient (zp 1), read through its tensor map
     uint32_t cin, cout, kp;
-    float *partial;  // [gridDim.x][kp][16]
+    float *partial;    // [gridDim.x][kp][16]
     uint32_t nblocks;
 };
 
-template <int NPLX, int NPLD>
+template <int NPLX>
 struct WgShape {
-    static constexpr uint32_t kXL = NPLX == 2 ? kWgLB + 3 : kWgLB + 8;  // y' lines per x'
-    static constexpr uint32_t kXLine = NPLX * 32 * 16;
-    static constexpr uint32_t kDLine = NPLD * 34 * 16;
-    // a single-plane gradient is read as N = 16 too: its second core matrix is the next
-    // line (columns 8..15 of D, unused), so one more line is staged
-    static constexpr uint32_t kDLines = NPLD == 2 ? kWgLB : kWgLB + 1;
-    static constexpr uint32_t kSlabX = kXL * kXLine;
-    static constexpr uint32_t kXBytes = 3 * kSlabX;
-    static constexpr uint32_t kDBytes = kDLines * kDLine;
-    static constexpr uint32_t kBuf = kXBytes + kDBytes;
-    static constexpr uint32_t kSmem = kOnesBytes + 2 * kBuf;
+    // staged activation lines y' = y0 .. y0 + kXL - 1, each as [dx][plane][32 voxels]: M-core
+    // i = (dy'' 3 + dx) planes + plane of output line j sits at (j planes 3 + i) x 512 B
+    static constexpr uint32_t kXL = NPLX == 2 ? kWgLB + 3 : kWgLB + 5;
+    static constexpr uint32_t kXLine = 3 * NPLX * 512;
+    static constexpr uint32_t kXBytes = kXL * kXLine;
+    static constexpr uint32_t kBBytes = kWgLB * kWgBLine;
+    static constexpr uint32_t kStage = kXBytes + kBBytes;
+    static constexpr uint32_t kSmem = kOnesBytes + kWgStages * kStage;
 };
 
 __device__ __forceinline__ void wg_block(uint32_t b, const Lp &g, uint32_t &s, uint32_t &x,
@@ -350,15 +354,36 @@ __device__ __forceinline__ void wg_block(uint32_t b, const Lp &g, uint32_t &s, u
     y0 = (r - x * per_x) * kWgLB;
 }
 
-template <int NPLX, int NPLD>
-__global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(WgradArgs a) {
-    using S = WgShape<NPLX, NPLD>;
+// Bounded wait that sleeps between polls (for threads with nothing else to do).
+__device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        __nanosleep(256);
+    }
+    return false;
+}
+
+// One block = 4 output lines of one (sample, x).  Per line j and K step (16 voxels):
+//   A (MN-major): the activation, staged [y'][dx][plane][32 voxels] by one TMA box, so
+//     M-core (dy'', dx, plane) -- channels 8 plane .. + 7 of line y + dy'' - 1 of x + dx - 1
+//     -- is at +512 B per core in the order (dy'', dx, plane), K groups of 8 voxels at
+//     +128 B.  Two planes: 18 useful cores = one M = 128 MMA (cores 0..15) and one M = 64
+//     (cores 16..23, of which 16 and 17 are used); one plane: 9 useful cores, one M = 128;
+//   B (MN-major, N = 48): the gradient line at three z shifts, staged as blocks
+//     (k, plane) of 32 rows starting at z' = k (k = 1 - dz) -- N-core (k, plane) at +512 B;
+// so D (48 columns: dz, co) accumulates two (one) MMAs per K step; the bias gradient is an
+// all-ones A against the k = 1 blocks.
+template <int NPLX>
+__global__ void __launch_bounds__(kWgThreads)
+    wgrad_tc_kernel(const __grid_constant__ CUtensorMap xmap,
+                    const __grid_constant__ CUtensorMap dymap, WgradArgs a) {
+    using S = WgShape<NPLX>;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t full[2], empty[2], done;
+    __shared__ __align__(8) uint64_t full[kWgStages], empty[kWgStages], done;
     __shared__ uint32_t taddr_s;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t *ones = smem;
-    uint8_t *buf_s = smem + kOnesBytes;
+    uint8_t *stage_s = smem + kOnesBytes;
 
     for (uint32_t i = tid; i < kOnesBytes / 4; i += kWgThreads)
         reinterpret_cast<uint32_t *>(ones)[i] = 0x3F803F80u;  // BF16 1.0 pairs
@@ -368,7 +393,7 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(WgradArgs a) {
         tmem_relinquish();
     }
     if (tid == 128) {
-        for (int i = 0; i < 2; i++) {
+        for (uint32_t i = 0; i < kWgStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
             mbar_init(smem_addr(&empty[i]), 1);
         }
@@ -382,95 +407,115 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(WgradArgs a) {
     const bool any = blockIdx.x < a.nblocks;
 
     if (tid == 128) {
-        auto copy = [&](uint32_t buf, uint32_t b) {
+        // ---- producer (TMA) and MMA issue, one thread
+        auto copy = [&](uint32_t st, uint32_t b) {
             uint32_t s, x, y0;
             wg_block(b, a.dy, s, x, y0);
-            const uint32_t bar = smem_addr(&full[buf]);
-            mbar_expect_tx(bar, S::kBuf);
-            const uint32_t dst = smem_addr(buf_s + buf * S::kBuf);
-            for (uint32_t dx = 0; dx < 3; dx++)
-                bulk_g2s(dst + dx * S::kSlabX, a.X + a.xin.row(s, x + dx, y0, 0, 0) * 16, S::kSlabX,
-                         bar);
-            bulk_g2s(dst + S::kXBytes, a.dY + a.dy.row(s, x + 1, y0 + 1, 0, 0) * 16, S::kDBytes, bar);
+            const uint32_t bar = smem_addr(&full[st]);
+            mbar_expect_tx(bar, S::kXBytes + kWgLB * 3 * a.dy.npl * 512);
+            const uint32_t dst = smem_addr(stage_s + st * S::kStage);
+            const int32_t xg = (int32_t)(s * (a.dy.n0 + 2) + x);
+            tma_load_4d(dst, &xmap, 0, 0, xg, (int32_t)y0, bar);
+            for (uint32_t j = 0; j < kWgLB; j++)
+                for (uint32_t k = 0; k < 3; k++)
+                    tma_load_4d(dst + S::kXBytes + j * kWgBLine + k * 1024, &dymap,
+                                (int32_t)(k * 8), 0, (int32_t)(y0 + 1 + j), xg + 1, bar);
             mbar_arrive(bar);
         };
-        const uint32_t idesc = umma_idesc_bf16(64, 16, true, true);
-        const uint32_t ones_a = smem_addr(ones);
+        const uint32_t idesc128 = umma_idesc_bf16(128, 48, true, true);
+        const uint32_t idesc64 = umma_idesc_bf16(64, 48, true, true);
+        const uint32_t idesc16 = umma_idesc_bf16(64, 16, true, true);
+        const uint64_t ones_d = umma_smem_desc(smem_addr(ones), 128, 256);
+        for (uint32_t i = 0; i < kWgStages; i++) {
+            const uint64_t b = blockIdx.x + (uint64_t)i * gridDim.x;
+            if (b >= a.nblocks) break;
+            copy(i, (uint32_t)b);
+        }
         uint32_t it = 0, acc = 0;
-        if (any) copy(0, blockIdx.x);
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
-            const uint32_t buf = it & 1, use = it >> 1;
-            if (!mbar_wait(smem_addr(&full[buf]), use & 1, kSpin)) {
+            const uint32_t st = it % kWgStages;
+            if (!mbar_wait(smem_addr(&full[st]), (it / kWgStages) & 1, kSpin)) {
                 fail(32);
                 break;
             }
             tc_fence_after();
-            const uint32_t xs = smem_addr(buf_s + buf * S::kBuf);
-            const uint32_t ds = xs + S::kXBytes;
+            const uint32_t xs = smem_addr(stage_s + st * S::kStage);
+            // descriptors of line 0, K step 0; later lines / steps add to the start field
+            const uint64_t ad0 = umma_smem_desc(xs, 128, 512);
+            const uint64_t bd0 = umma_smem_desc(xs + S::kXBytes, 128, 512);
+#pragma unroll 1
             for (uint32_t j = 0; j < kWgLB; j++) {
+#pragma unroll
                 for (uint32_t ks = 0; ks < 2; ks++) {
-                    for (uint32_t dx = 0; dx < 3; dx++) {
-                        const uint64_t ad = umma_smem_desc(
-                            xs + dx * S::kSlabX + j * S::kXLine + ks * 256, 128, 512);
-                        for (uint32_t dz = 0; dz < 3; dz++) {
-                            const uint64_t bd = umma_smem_desc(
-                                ds + j * S::kDLine + (2 - dz) * 16 + ks * 256, 128, S::kDLine / NPLD);
-                            umma_bf16(taddr + (dx * 3 + dz) * 16, ad, bd, idesc, acc);
-                        }
-                    }
-                    umma_bf16(taddr + 9 * 16, umma_smem_desc(ones_a, 128, 256),
-                              umma_smem_desc(ds + j * S::kDLine + 16 + ks * 256, 128, S::kDLine / NPLD),
-                              idesc, acc);
+                    const uint64_t bd = bd0 + ((j * kWgBLine + ks * 256) >> 4);
+                    const uint64_t ad = ad0 + ((j * S::kXLine + ks * 256) >> 4);
+                    umma_bf16(taddr, ad, bd, idesc128, acc);
+                    if (NPLX == 2) umma_bf16(taddr + kWgAcc64, ad + ((16 * 512) >> 4), bd, idesc64, acc);
+                    umma_bf16(taddr + kWgBias, ones_d, bd + (1024 >> 4), idesc16, acc);
                     acc = 1;
                 }
             }
-            umma_commit(smem_addr(&empty[buf]));
-            const uint32_t nb = b + gridDim.x;
-            if (nb < a.nblocks) {
-                const uint32_t nbuf = (it + 1) & 1, nuse = (it + 1) >> 1;
-                if (nuse > 0 && !mbar_wait(smem_addr(&empty[nbuf]), (nuse - 1) & 1, kSpin)) {
-                    fail(64);
-                    break;
+            umma_commit(smem_addr(&empty[st]));
+            // refill the previous block's stage with the block kWgStages after it
+            if (it >= 1) {
+                const uint32_t old = it - 1;
+                const uint64_t pb = blockIdx.x + (uint64_t)(old + kWgStages) * gridDim.x;
+                if (pb < a.nblocks) {
+                    const uint32_t ps = old % kWgStages;
+                    if (!mbar_wait(smem_addr(&empty[ps]), (old / kWgStages) & 1, kSpin)) {
+                        fail(64);
+                        break;
+                    }
+                    copy(ps, (uint32_t)pb);
                 }
-                copy(nbuf, nb);
             }
         }
         umma_commit(smem_addr(&done));
     } else if (tid < 128) {
         float *P = a.partial + (uint64_t)blockIdx.x * a.kp * 16;
-        const bool ok = mbar_wait(smem_addr(&done), 0, kSpin * 4);
+        const bool ok = mbar_wait_sleep(smem_addr(&done), 0, kSpin);
         if (!ok) fail(128);
         tc_fence_after();
         if (!any || !ok) {
             for (uint32_t i = tid; i < a.kp * 16; i += 128) P[i] = 0.0f;
         } else {
-            for (uint32_t ai = 0; ai < 10; ai++) {
+            // chunk c: 0..2 = M = 128 accumulator (k = c), 3..5 = M = 64 (k = c - 3), 6 = bias
+            const uint32_t chunks = NPLX == 2 ? 7 : 4;
+            for (uint32_t c = 0; c < chunks; c++) {
+                const bool bias = c == chunks - 1;
+                const bool m64 = !bias && c >= 3;
                 float v[16];
                 __syncwarp();
-                tmem_ld16(taddr + ((warp * 32u) << 16) + ai * 16, v);
+                tmem_ld16(taddr + ((warp * 32u) << 16) +
+                              (bias ? kWgBias : m64 ? kWgAcc64 + (c - 3) * 16 : c * 16), v);
                 tmem_ld_wait();
                 uint32_t row = 0;
-                bool valid = false;
-                if (ai < 9) {
-                    uint32_t dyi, ci;
-                    if (NPLX == 2) {
-                        dyi = warp;
-                        ci = lane;
-                    } else {
-                        const uint32_t r = 16 * warp + lane;
-                        dyi = r / 8;
-                        ci = r % 8;
-                    }
-                    valid = lane < 16 && dyi < 3 && ci < a.cin;
-                    row = ((ai / 3) * 9 + dyi * 3 + ai % 3) * a.cin + ci;
-                } else {
+                bool valid;
+                if (bias) {
                     valid = warp == 0 && lane == 0;
                     row = 27 * a.cin;
+                } else {
+                    // accumulator row -> M-core i and channel within the core
+                    uint32_t i, c8;
+                    if (m64) {
+                        valid = lane < 16;
+                        i = 16 + (warp * 16 + lane) / 8;
+                        c8 = lane % 8;
+                    } else {
+                        valid = true;
+                        i = (warp * 32 + lane) / 8;
+                        c8 = lane % 8;
+                    }
+                    const uint32_t dyi = i / (3 * NPLX), dx = (i / NPLX) % 3, h = i % NPLX;
+                    const uint32_t ci = h * 8 + c8;
+                    const uint32_t dzi = 2 - (m64 ? c - 3 : c);  // chunk k holds dz = 1 - k
+                    valid = valid && dyi < 3 && ci < a.cin;
+                    row = (dx * 9 + dyi * 3 + dzi) * a.cin + ci;
                 }
                 if (valid) {
                     float *p = P + (uint64_t)row * 16;
 #pragma unroll
-                    for (int c = 0; c < 16; c++) p[c] = c < NPLD * 8 ? v[c] : 0.0f;
+                    for (int co = 0; co < 16; co++) p[co] = co < (int)(a.dy.npl * 8) ? v[co] : 0.0f;
                 }
             }
         }
@@ -484,16 +529,24 @@ __global__ void __launch_bounds__(kWgThreads) wgrad_tc_kernel(WgradArgs a) {
 }
 
 // dW[k][n] = sum over CTAs of partial[p][k][n] (k <= 27 cin), 0 on the padding rows.
-__global__ void wgrad_tc_reduce_kernel(const float *__restrict__ partial, uint32_t parts,
-                                       uint32_t kp, uint32_t cin, uint32_t cout,
-                                       float *__restrict__ dW) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp * cout) return;
-    const uint32_t k = i / cout, n = i % cout;
+// One CTA per row k: thread (p0, n) sums p = p0, p0 + 16, ... in order, then a fixed tree
+// over p0 (deterministic).
+__global__ void __launch_bounds__(256) wgrad_tc_reduce_kernel(const float *__restrict__ partial,
+                                                              uint32_t parts, uint32_t kp,
+                                                              uint32_t cin, uint32_t cout,
+                                                              float *__restrict__ dW) {
+    __shared__ float red[16][17];
+    const uint32_t k = blockIdx.x, n = threadIdx.x % 16, p0 = threadIdx.x / 16;
     float s = 0.0f;
     if (k <= 27 * cin)
-        for (uint32_t p = 0; p < parts; p++) s += partial[((uint64_t)p * kp + k) * 16 + n];
-    dW[i] = s;
+        for (uint32_t p = p0; p < parts; p += 16) s += partial[((uint64_t)p * kp + k) * 16 + n];
+    red[p0][n] = s;
+    __syncthreads();
+    for (uint32_t w = 8; w > 0; w >>= 1) {
+        if (p0 < w) red[p0][n] += red[p0 + w][n];
+        __syncthreads();
+    }
+    if (p0 == 0 && n < cout) dW[(uint64_t)k * cout + n] = red[0][n];
 }
 
 // ---- layout conversion, weights, loss ----------------------------------------------------
@@ -536,28 +589,66 @@ __global__ void lp_unpack_kernel(const uint8_t *__restrict__ in, Lp g, uint32_t 
     }
 }
 
-// Weight image of a convolution with `in_ch` input channels (groups x 2 KB): element
-// (group g, row m = dz 16 + oc, column k) at g 2048 + (k/8) 1024 + (m/8) 128 + (m%8) 16 +
-// (k%8) 2; column k = input channel (two planes) or (tap of the pair, channel) for one
-// plane.  Forward: W[t cin + ic][oc]; backward-data: W[(26 - t) cin + oc][ic].
+// Weight image of a convolution with `in_ch` input channels (groups x 1536 B, the B
+// operand, K-major): element (group g, row n = dz 16 + oc, column k) at g 1536 +
+// (k/8) 768 + (n/8) 128 + (n%8) 16 + (k%8) 2; column k = input channel (two planes) or
+// (tap of the pair, channel) for one plane.  Forward: W[t cin + ic][oc]; backward-data:
+// W[(26 - t) cin + oc][ic].
 __global__ void pack_tc_weights_kernel(const float *__restrict__ W, uint32_t cin, uint32_t cout,
                                        int backward, uint32_t groups,
                                        __nv_bfloat16 *__restrict__ img) {
     const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= groups * 1024) return;
-    const uint32_t g = e / 1024, m = (e / 16) % 64, k = e % 16;
+    if (e >= groups * kConvN * 16) return;
+    const uint32_t g = e / (kConvN * 16), n = (e / 16) % kConvN, k = e % 16;
     const uint32_t in_ch = backward ? cout : cin, out_ch = backward ? cin : cout;
     const bool two = in_ch > 8;
     const uint32_t tap9 = two ? g : 2 * g + k / 8, ic = two ? k : k % 8;
-    const uint32_t dz = m / 16, oc = m % 16;
+    const uint32_t dz = n / 16, oc = n % 16;
     float w = 0.0f;
-    if (tap9 < 9 && m < 48 && ic < in_ch && oc < out_ch) {
+    if (tap9 < 9 && ic < in_ch && oc < out_ch) {
         const uint32_t t = (tap9 / 3) * 9 + (tap9 % 3) * 3 + dz;
         w = backward ? W[((uint64_t)(26 - t) * cin + oc) * cout + ic]
                      : W[((uint64_t)t * cin + ic) * cout + oc];
     }
-    const uint32_t off = g * 2048 + (k / 8) * 1024 + (m / 8) * 128 + (m % 8) * 16 + (k % 8) * 2;
+    const uint32_t off = g * kConvGroup + (k / 8) * (kConvN * 16) + (n / 8) * 128 + (n % 8) * 16 +
+                         (k % 8) * 2;
     img[off / 2] = __float2bfloat16_rn(w);
+}
+
+// Several images in one launch: job j packs W[j / 2] forward (j even) or backward-data
+// (j odd, when img[j] is non-null); element e of the launch belongs to the job whose range
+// [start[j], start[j + 1]) holds it.
+constexpr uint32_t kMaxPackJobs = 16;
+struct PackJobs {
+    const float *W[kMaxPackJobs];
+    __nv_bfloat16 *img[kMaxPackJobs];
+    uint32_t cin[kMaxPackJobs], cout[kMaxPackJobs], groups[kMaxPackJobs];
+    uint32_t start[kMaxPackJobs + 1];
+    uint32_t jobs;
+};
+
+__global__ void pack_tc_jobs_kernel(PackJobs p) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p.start[p.jobs]) return;
+    uint32_t j = 0;
+    while (e >= p.start[j + 1]) j++;
+    const uint32_t q = e - p.start[j];
+    const uint32_t g = q / (kConvN * 16), n = (q / 16) % kConvN, k = q % 16;
+    const bool backward = j & 1;
+    const uint32_t cin = p.cin[j], cout = p.cout[j];
+    const uint32_t in_ch = backward ? cout : cin, out_ch = backward ? cin : cout;
+    const bool two = in_ch > 8;
+    const uint32_t tap9 = two ? g : 2 * g + k / 8, ic = two ? k : k % 8;
+    const uint32_t dz = n / 16, oc = n % 16;
+    float w = 0.0f;
+    if (tap9 < 9 && ic < in_ch && oc < out_ch) {
+        const uint32_t t = (tap9 / 3) * 9 + (tap9 % 3) * 3 + dz;
+        w = backward ? p.W[j][((uint64_t)(26 - t) * cin + oc) * cout + ic]
+                     : p.W[j][((uint64_t)t * cin + ic) * cout + oc];
+    }
+    const uint32_t off = g * kConvGroup + (k / 8) * (kConvN * 16) + (n / 8) * 128 + (n % 8) * 16 +
+                         (k % 8) * 2;
+    p.img[j][off / 2] = __float2bfloat16_rn(w);
 }
 
 // dZ (single-plane gradient, zp 1) and the per-voxel loss of BCE-with-logits:
@@ -608,13 +699,6 @@ int sm_count_cached() {
     return n > 0 ? n : 148;
 }
 
-template <typename K>
-int set_smem(K kernel, uint32_t bytes) {
-    BPGB_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)bytes));
-    return BPGB_OK;
-}
-
 unsigned grid_for(uint64_t n, unsigned threads, unsigned cap) {
     const uint64_t b = (n + threads - 1) / threads;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(b, cap));
@@ -638,7 +722,7 @@ uint64_t bpgb_cnn_lp_bytes(uint32_t channels, uint32_t zpad, const uint32_t *dim
 
 uint64_t bpgb_cnn_tc_weight_bytes(uint32_t in_channels) {
     if (in_channels == 0 || in_channels > 16) return 0;
-    return (in_channels > 8 ? 9u : 5u) * 2048u;
+    return (in_channels > 8 ? 9u : 5u) * kConvGroup;
 }
 
 int bpgb_cnn_lp_pack(const void *d_X, uint32_t channels, uint32_t x_stride, const uint32_t *dims,
@@ -678,16 +762,47 @@ int bpgb_cnn_tc_pack_weights(const float *d_W, uint32_t cin, uint32_t cout, void
         (d_Wb && !aligned16(d_Wb)))
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad tc_pack_weights arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    const uint32_t gf = (uint32_t)(bpgb_cnn_tc_weight_bytes(cin) / 2048);
-    pack_tc_weights_kernel<<<(gf * 1024 + 255) / 256, 256, 0, s>>>(d_W, cin, cout, 0, gf,
-                                                                   (__nv_bfloat16 *)d_Wf);
+    const uint32_t gf = (uint32_t)(bpgb_cnn_tc_weight_bytes(cin) / kConvGroup);
+    pack_tc_weights_kernel<<<(gf * kConvN * 16 + 255) / 256, 256, 0, s>>>(
+        d_W, cin, cout, 0, gf, (__nv_bfloat16 *)d_Wf);
     count_launches(1);
     if (d_Wb) {
-        const uint32_t gb = (uint32_t)(bpgb_cnn_tc_weight_bytes(cout) / 2048);
-        pack_tc_weights_kernel<<<(gb * 1024 + 255) / 256, 256, 0, s>>>(d_W, cin, cout, 1, gb,
-                                                                       (__nv_bfloat16 *)d_Wb);
+        const uint32_t gb = (uint32_t)(bpgb_cnn_tc_weight_bytes(cout) / kConvGroup);
+        pack_tc_weights_kernel<<<(gb * kConvN * 16 + 255) / 256, 256, 0, s>>>(
+            d_W, cin, cout, 1, gb, (__nv_bfloat16 *)d_Wb);
         count_launches(1);
     }
+    BPGB_CUDA_TRY(cudaGetLastError());
+    return BPGB_OK;
+}
+
+int bpgb_cnn_tc_pack_layers(const float *const *d_W, const uint32_t *cin, const uint32_t *cout,
+                            void *const *d_Wf, void *const *d_Wb, uint32_t layers, void *stream) {
+    clear_error();
+    if (!d_W || !cin || !cout || !d_Wf || layers == 0 || 2 * layers > kMaxPackJobs)
+        return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad tc_pack_layers arguments (1..8 layers)");
+    PackJobs p{};
+    uint32_t n = 0;
+    for (uint32_t l = 0; l < layers; l++) {
+        if (!d_W[l] || !d_Wf[l] || cin[l] == 0 || cin[l] > 16 || cout[l] == 0 || cout[l] > 16 ||
+            !aligned16(d_Wf[l]) || (d_Wb && d_Wb[l] && !aligned16(d_Wb[l])))
+            return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad tc_pack_layers layer");
+        for (uint32_t b = 0; b < 2; b++) {
+            void *img = b ? (d_Wb ? d_Wb[l] : nullptr) : d_Wf[l];
+            const uint32_t j = 2 * l + b;
+            p.W[j] = d_W[l];
+            p.img[j] = (__nv_bfloat16 *)img;
+            p.cin[j] = cin[l];
+            p.cout[j] = cout[l];
+            p.groups[j] = img ? (uint32_t)(bpgb_cnn_tc_weight_bytes(b ? cout[l] : cin[l]) / kConvGroup) : 0;
+            p.start[j] = n;
+            n += p.groups[j] * kConvN * 16;
+        }
+    }
+    p.jobs = 2 * layers;
+    p.start[p.jobs] = n;
+    pack_tc_jobs_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(p);
+    count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
 }
@@ -705,7 +820,22 @@ int bpgb_cnn_tc_conv3d(const void *d_X, uint32_t in_channels, uint32_t in_zpad,
         return set_error(BPGB_ERR_INVALID_ARGUMENT,
                          "bad tc_conv3d arguments (channels 1..16, dims[2] = 32, dims[1] % 8 = 0, "
                          "16-byte aligned tensors)");
-    a.X = (const uint8_t *)d_X;
+    if (!tensor_map_encoder()) return set_error(BPGB_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    // the input as [x' (with sample)][y'][plane][z' x 8 channels]: boxes of 7 lines x the
+    // line's 32 voxels (256 elements, 512 B contiguous) of one plane
+    const Lp &g = a.in;
+    const cuuint64_t gdims[4] = {g.L() * 8ull, g.npl, g.n1 + 2ull, (cuuint64_t)batch * (g.n0 + 2)};
+    const cuuint64_t gstr[3] = {g.L() * 16ull, (cuuint64_t)g.line_rows() * 16,
+                                (g.n1 + 2ull) * g.line_rows() * 16};
+    const cuuint32_t box[4] = {256, 1, kConvLines, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUtensorMap map;
+    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                                      const_cast<void *>(d_X), gdims, gstr, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (cnn)");
     a.W = (const uint8_t *)d_W;
     a.bias = d_bias;
     a.cout = out_channels;
@@ -714,18 +844,18 @@ int bpgb_cnn_tc_conv3d(const void *d_X, uint32_t in_channels, uint32_t in_zpad,
     a.Y = (uint8_t *)d_Y;
     a.Yf = d_Yf;
     a.nblocks = batch * dims[0] * (dims[1] / kConvLB);
-    const unsigned grid = (unsigned)std::min<uint64_t>(a.nblocks, 2ull * sm_count_cached());
     cudaStream_t s = (cudaStream_t)stream;
     int st;
-    if (a.in.npl == 2) {
-        const uint32_t sm = std::max(kMinSmem, ConvShape<2>::smem(in_zpad));
-        if ((st = set_smem(conv_tc_kernel<2>, sm))) return st;
-        conv_tc_kernel<2><<<grid, kConvThreads, sm, s>>>(a);
-    } else {
-        const uint32_t sm = std::max(kMinSmem, ConvShape<1>::smem(in_zpad));
-        if ((st = set_smem(conv_tc_kernel<1>, sm))) return st;
-        conv_tc_kernel<1><<<grid, kConvThreads, sm, s>>>(a);
-    }
+    auto launch = [&](auto kernel, uint32_t smem) -> int {
+        smem = std::max(kMinSmem, smem);
+        if ((st = reserve_dynamic_smem((const void *)kernel, smem))) return st;
+        const unsigned grid = (unsigned)std::min<uint64_t>(a.nblocks, 2ull * sm_count_cached());
+        kernel<<<grid, kConvThreads, smem, s>>>(map, a);
+        return BPGB_OK;
+    };
+    st = a.in.npl == 2 ? launch(conv_tc_kernel<2>, ConvShape<2>::kSmem)
+                       : launch(conv_tc_kernel<1>, ConvShape<1>::kSmem);
+    if (st) return st;
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;
@@ -750,8 +880,36 @@ int bpgb_cnn_tc_conv3d_wgrad(const void *d_X, uint32_t in_channels, const void *
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad tc_conv3d_wgrad arguments");
     if (scratch_bytes < bpgb_cnn_tc_wgrad_scratch_bytes(in_channels, dims, batch))
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "tc wgrad scratch too small");
-    a.X = (const uint8_t *)d_X;
-    a.dY = (const uint8_t *)d_dY;
+    if (!tensor_map_encoder()) return set_error(BPGB_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    // the gradient as [x' (with sample)][y'][plane][z' x 8 channels]: boxes of one line's
+    // planes x 32 rows (256 elements) starting at row k
+    const Lp &g = a.dy;
+    const cuuint64_t gdims[4] = {g.L() * 8ull, g.npl, g.n1 + 2ull, (cuuint64_t)batch * (g.n0 + 2)};
+    const cuuint64_t gstr[3] = {g.L() * 16ull, (cuuint64_t)g.line_rows() * 16,
+                                (g.n1 + 2ull) * g.line_rows() * 16};
+    const cuuint32_t box[4] = {256, g.npl, 1, 1};
+    // the activation as [y'][x' (with sample)][plane][32 voxels x 8 channels] (dimension 2 is
+    // x', dimension 3 y'): one box = 3 x' x the staged y' lines, landing [y'][dx][plane][z]
+    const Lp &gx = a.xin;
+    const cuuint64_t xdims[4] = {256, gx.npl, (cuuint64_t)batch * (gx.n0 + 2), gx.n1 + 2ull};
+    const cuuint64_t xstr[3] = {512, (gx.n1 + 2ull) * gx.line_rows() * 16,
+                                (cuuint64_t)gx.line_rows() * 16};
+    const cuuint32_t xbox[4] = {256, gx.npl, 3,
+                                gx.npl == 2 ? WgShape<2>::kXL : WgShape<1>::kXL};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUtensorMap map, xmap;
+    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                                      const_cast<void *>(d_dY), gdims, gstr, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS)
+        r = tensor_map_encoder()(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                                 const_cast<void *>(d_X), xdims, xstr, xbox, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(BPGB_ERR_CUDA, "cuTensorMapEncodeTiled failed (cnn wgrad)");
     a.cin = in_channels;
     a.cout = out_channels;
     a.kp = bpgb_cnn_kp(in_channels);
@@ -760,20 +918,18 @@ int bpgb_cnn_tc_conv3d_wgrad(const void *d_X, uint32_t in_channels, const void *
     const unsigned grid = (unsigned)std::min<uint64_t>(a.nblocks, 2ull * sm_count_cached());
     cudaStream_t s = (cudaStream_t)stream;
     int st;
-#define BPGB_WG(PX, PD)                                                                \
-    do {                                                                               \
-        const uint32_t sm = std::max(kMinSmem, WgShape<PX, PD>::kSmem);                \
-        if ((st = set_smem(wgrad_tc_kernel<PX, PD>, sm))) return st;                   \
-        wgrad_tc_kernel<PX, PD><<<grid, kWgThreads, sm, s>>>(a);                       \
-    } while (0)
-    if (a.xin.npl == 2 && a.dy.npl == 2) BPGB_WG(2, 2);
-    else if (a.xin.npl == 2) BPGB_WG(2, 1);
-    else if (a.dy.npl == 2) BPGB_WG(1, 2);
-    else BPGB_WG(1, 1);
-#undef BPGB_WG
+    auto launch = [&](auto kernel, uint32_t smem) -> int {
+        smem = std::max(kMinSmem, smem);
+        if ((st = reserve_dynamic_smem((const void *)kernel, smem))) return st;
+        kernel<<<grid, kWgThreads, smem, s>>>(xmap, map, a);
+        return BPGB_OK;
+    };
+    st = a.xin.npl == 2 ? launch(wgrad_tc_kernel<2>, WgShape<2>::kSmem)
+                        : launch(wgrad_tc_kernel<1>, WgShape<1>::kSmem);
+    if (st) return st;
     count_launches(1);
-    wgrad_tc_reduce_kernel<<<(a.kp * out_channels + 255) / 256, 256, 0, s>>>(
-        d_scratch, grid, a.kp, in_channels, out_channels, d_dW);
+    wgrad_tc_reduce_kernel<<<a.kp, 256, 0, s>>>(d_scratch, grid, a.kp, in_channels, out_channels,
+                                                d_dW);
     count_launches(1);
     BPGB_CUDA_TRY(cudaGetLastError());
     return BPGB_OK;

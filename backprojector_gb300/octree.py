@@ -70,8 +70,8 @@ class OccupancyCNN:
             in_channels = int(state["in_channels"])
         self.in_channels = in_channels
         self.layers = layers(in_channels)
-        self.W, self.M, self.V = [], [], []
         rng = np.random.default_rng(seed)
+        ws = []
         for li, (cin, cout, _) in enumerate(self.layers):
             kp = capi.cnn_kp(cin)
             if state is not None:
@@ -81,9 +81,16 @@ class OccupancyCNN:
                 w = np.zeros((kp, cout), np.float32)
                 fan_in = 27 * cin
                 w[:27 * cin] = rng.normal(0.0, math.sqrt(2.0 / fan_in), (27 * cin, cout))
-            self.W.append(torch.from_numpy(w).to(device))
-            self.M.append(torch.zeros_like(self.W[-1]))
-            self.V.append(torch.zeros_like(self.W[-1]))
+            ws.append(w)
+        # masters, Adam moments and gradients: one flat buffer each (one Adam launch), the
+        # layers as views [KP][COUT] into it
+        self.shapes = [w.shape for w in ws]
+        self.flat_W = torch.from_numpy(np.concatenate([w.reshape(-1) for w in ws])).to(device)
+        self.flat_M = torch.zeros_like(self.flat_W)
+        self.flat_V = torch.zeros_like(self.flat_W)
+        self.flat_G = torch.zeros_like(self.flat_W)
+        self.W, self.M, self.V, self.G = (self._views(f) for f in (
+            self.flat_W, self.flat_M, self.flat_V, self.flat_G))
         self.step = int(state["step"]) if state is not None and "step" in state else 0
         self.Wt, self.Wb = [], []
         for li, (cin, cout, _) in enumerate(self.layers):
@@ -91,14 +98,45 @@ class OccupancyCNN:
                                        device=device))
             self.Wb.append(torch.zeros((16, capi.cnn_kp(cout)), dtype=torch.bfloat16,
                                        device=device) if li > 0 else None)
+        # tensor-core (tcgen05) weight images of the training step: forward, backward-data
+        self.Wtc, self.Wtc_b = [], []
+        for li, (cin, cout, _) in enumerate(self.layers):
+            self.Wtc.append(torch.zeros(capi.cnn_tc_weight_bytes(cin) // 2, dtype=torch.bfloat16,
+                                        device=device))
+            self.Wtc_b.append(torch.zeros(capi.cnn_tc_weight_bytes(cout) // 2,
+                                          dtype=torch.bfloat16, device=device)
+                              if li > 0 else None)
         self._bufs = {}
+        self._mma_stale = False
         self.pack()
+
+    def _views(self, flat):
+        out, off = [], 0
+        for kp, cout in self.shapes:
+            out.append(flat[off:off + kp * cout].view(kp, cout))
+            off += kp * cout
+        return out
 
     # ---- weights
     def pack(self, stream=None):
+        self.pack_mma(stream)
+        self.pack_tc(stream)
+
+    def pack_mma(self, stream=None):
+        """BF16 images of the inference kernels (bpgb_cnn_conv3d)."""
         for li, (cin, cout, _) in enumerate(self.layers):
             capi.cnn_pack_weights(self.W[li], cin, cout, _np(cout), self.Wt[li],
                                   16 if li > 0 else 0, self.Wb[li], stream)
+        self._mma_stale = False
+
+    def pack_tc(self, stream=None):
+        """BF16 images of the tensor-core training kernels (bpgb_cnn_tc_conv3d), one launch."""
+        capi.cnn_tc_pack_layers(self.W, [l[0] for l in self.layers], [l[1] for l in self.layers],
+                                self.Wtc, self.Wtc_b, stream)
+
+    def bias(self, li: int):
+        """FP32 bias row of layer li (a view into the master weights)."""
+        return self.W[li][27 * self.layers[li][0]]
 
     def state(self) -> dict:
         d = {f"w{li}": self.W[li].cpu().numpy() for li in range(len(self.layers))}
@@ -141,6 +179,8 @@ class OccupancyCNN:
     def forward(self, X0, dims, batch: int, logits=None, stream=None):
         """logits (FP32 [batch * prod(dims)]) of input features X0 (features())."""
         torch = self.torch
+        if self._mma_stale:
+            self.pack_mma(stream)
         V = batch * int(np.prod(dims))
         Y1 = self._buf("Y1", (V, 16), torch.bfloat16)
         Y2 = self._buf("Y2", (V, 16), torch.bfloat16)
@@ -154,9 +194,78 @@ class OccupancyCNN:
         capi.cnn_conv3d(Y3, 16, 16, dims, batch, self.Wt[3], 8, False, d_Yf=logits, stream=stream)
         return logits
 
+    def _lp(self, name, channels, zpad, dims, batch):
+        """A line-planes tensor, cleared once when (re)allocated: its padding rows stay 0."""
+        n = capi.cnn_lp_bytes(channels, zpad, dims, batch) // 2
+        t = self._bufs.get(name)
+        if t is None or t.numel() != n:
+            t = self.torch.zeros(n, dtype=self.torch.bfloat16, device=self.device)
+            self._bufs[name] = t
+        return t
+
+    def tc_supported(self, dims) -> bool:
+        """The tensor-core kernels take z-lines of 32 voxels and n1 % 8 == 0."""
+        return int(dims[2]) == 32 and int(dims[1]) % 8 == 0
+
     def train_step(self, X0, labels, dims, batch: int, lr: float, pos_weight: float,
-                   stream=None):
-        """One Adam step on BCE-with-logits; returns the loss tensor (per voxel)."""
+                   stream=None, tc: bool | None = None):
+        """One Adam step on BCE-with-logits; returns the loss tensor (per voxel).
+
+        Runs on the tcgen05 kernels (bpgb_cnn_tc_*) when the volume allows it (tc=None),
+        else, or with tc=False, on the mma.sync kernels (bpgb_cnn_conv3d*)."""
+        if tc is None:
+            tc = self.tc_supported(dims)
+        if tc:
+            return self._train_step_tc(X0, labels, dims, batch, lr, pos_weight, stream)
+        return self._train_step_mma(X0, labels, dims, batch, lr, pos_weight, stream)
+
+    def _train_step_tc(self, X0, labels, dims, batch, lr, pos_weight, stream):
+        torch = self.torch
+        V = batch * int(np.prod(dims))
+        ci = self.in_channels
+        X0l = self._lp("X0l", ci, 0, dims, batch)
+        Yl = [self._lp(f"Y{i}l", 16, 0, dims, batch) for i in (1, 2, 3)]
+        dZl = self._lp("dZl", 1, 1, dims, batch)
+        dYl = [self._lp(f"dY{i}l", 16, 1, dims, batch) for i in (1, 2, 3)]
+        logits = self._buf("Z", (V,), torch.float32)
+        loss = self._buf("loss", (V,), torch.float32)
+        G = self.G
+        nscr = max(capi.cnn_tc_wgrad_scratch_bytes(16, dims, batch),
+                   capi.cnn_tc_wgrad_scratch_bytes(ci, dims, batch))
+        scr = self._buf("tc_scratch", (nscr // 4,), torch.float32)
+        conv, wgrad = capi.cnn_tc_conv3d, capi.cnn_tc_conv3d_wgrad
+        capi.cnn_lp_pack(X0, ci, ci, dims, batch, 0, X0l, stream)
+        # forward
+        ins = [X0l] + Yl
+        for li, (cin, cout, relu) in enumerate(self.layers):
+            if li < 3:
+                conv(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout, relu,
+                     d_Y=Yl[li], stream=stream)
+            else:
+                conv(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout, False,
+                     d_Yf=logits, stream=stream)
+        capi.cnn_tc_bce_grad(logits, labels, dims, batch, pos_weight, 1.0 / V, dZl, loss, stream)
+        # backward: weight gradient of layer li, then the input gradient (masked by the
+        # ReLU of the layer below)
+        grads = [dYl[0], dYl[1], dYl[2], dZl]
+        for li in (3, 2, 1, 0):
+            cin, cout, _ = self.layers[li]
+            wgrad(ins[li], cin, grads[li], cout, dims, batch, scr, nscr, G[li], stream)
+            if li > 0:
+                conv(grads[li], cout, 1, dims, batch, self.Wtc_b[li], None, cin, False,
+                     d_mask=Yl[li - 1], d_Y=dYl[li - 1], out_zpad=1, stream=stream)
+        self._adam(lr, stream)
+        self.pack_tc(stream)
+        self._mma_stale = True
+        return loss
+
+    def _adam(self, lr, stream):
+        """One Adam step of every layer (the flat buffers) on the gradients in self.G."""
+        self.step += 1
+        capi.cnn_adam(self.flat_W, self.flat_G, self.flat_M, self.flat_V, self.flat_W.numel(), lr,
+                      0.9, 0.999, 1e-8, self.step, stream)
+
+    def _train_step_mma(self, X0, labels, dims, batch, lr, pos_weight, stream):
         torch = self.torch
         V = batch * int(np.prod(dims))
         logits = self.forward(X0, dims, batch, stream=stream)
@@ -167,8 +276,7 @@ class OccupancyCNN:
         dY3 = self._buf("dY3", (V, 16), torch.bfloat16)
         dY2 = self._buf("dY2", (V, 16), torch.bfloat16)
         dY1 = self._buf("dY1", (V, 16), torch.bfloat16)
-        G = [self._buf(f"g{li}", tuple(self.W[li].shape), torch.float32)
-             for li in range(len(self.layers))]
+        G = self.G
         ci = self.in_channels
         nscr = max(capi.cnn_wgrad_scratch_bytes(16, 16, dims, batch),
                    capi.cnn_wgrad_scratch_bytes(ci, 16, dims, batch))
@@ -183,10 +291,7 @@ class OccupancyCNN:
         capi.cnn_conv3d(dY2, 16, 16, dims, batch, self.Wb[1], 16, False, d_Y=dY1, d_mask=Y1,
                         mask_stride=16, stream=stream)
         capi.cnn_conv3d_wgrad(X0, ci, ci, dims, batch, dY1, 16, 16, scr, nscr, G[0], stream)
-        self.step += 1
-        for li in range(len(self.layers)):
-            capi.cnn_adam(self.W[li], G[li], self.M[li], self.V[li], self.W[li].numel(), lr, 0.9,
-                          0.999, 1e-8, self.step, stream)
+        self._adam(lr, stream)
         self.pack(stream)
         return loss
 

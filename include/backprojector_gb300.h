@@ -431,6 +431,10 @@ int bpgb_cnn_lp_unpack(const void *d_lp, uint32_t channels, uint32_t zpad, const
  * channels transposed) into d_Wb when non-null. */
 int bpgb_cnn_tc_pack_weights(const float *d_W, uint32_t cin, uint32_t cout, void *d_Wf,
                              void *d_Wb, void *stream);
+/* bpgb_cnn_tc_pack_weights for `layers` (<= 8) layers in one launch: host arrays of the
+ * layers' masters, channel counts and image pointers (d_Wb or its entries may be null). */
+int bpgb_cnn_tc_pack_layers(const float *const *d_W, const uint32_t *cin, const uint32_t *cout,
+                            void *const *d_Wf, void *const *d_Wb, uint32_t layers, void *stream);
 /* 3x3x3 convolution, zero padding: Y = act(conv(X) + bias) on the tensor cores.  d_bias
  * (out_channels FP32, or null), relu, d_mask (an activation-layout tensor of out_channels:
  * outputs where mask <= 0 are zeroed -- the ReLU derivative of the backward pass), d_Y

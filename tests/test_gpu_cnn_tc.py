@@ -185,3 +185,52 @@ def test_tc_bce_matches_channels_last(cuda):
     got = from_lp(dzl, 1, 1, cuda)
     assert torch.equal(got[:, 0], dZ[:, 0].float().cpu())
     assert torch.equal(loss2.cpu(), loss.cpu())
+
+
+def test_tc_train_step_matches_mma_step(cuda):
+    """One training step of the 4-layer CNN on the tensor-core kernels against the same
+    step on the mma.sync kernels, from the same weights and inputs (batch 4 of 32^3):
+    per-voxel losses and every layer's weight gradient agree to BF16 rounding of the
+    activations (summation orders differ)."""
+    import torch
+
+    from backprojector_gb300 import octree
+
+    dims, batch = (32, 32, 32), 4
+    g = torch.Generator().manual_seed(0)
+    coarse = torch.rand((batch, 32 ** 3), generator=g).to(cuda)
+    y = (torch.rand(batch * 32 ** 3, generator=g) < 0.1).to(torch.uint8).to(cuda)
+    ma, mb = octree.OccupancyCNN(cuda, seed=0), octree.OccupancyCNN(cuda, seed=0)
+    X = ma.features(coarse, dims, batch)
+    la = ma.train_step(X, y, dims, batch, 1e-3, 10.0, tc=True)
+    lb = mb.train_step(X, y, dims, batch, 1e-3, 10.0, tc=False)
+    torch.cuda.synchronize()
+    assert capi.cnn_tc_status() == 0
+    la, lb = la.double().cpu(), lb.double().cpu()
+    assert float((la - lb).norm() / lb.norm()) < 1e-2
+    for li in range(4):
+        ga, gb = ma.G[li].double().cpu(), mb.G[li].double().cpu()
+        rel = float((ga - gb).norm() / gb.norm())
+        print(f"\nlayer {li}: weight-gradient rel-L2 tc vs mma.sync {rel:.2e}")
+        assert rel < 2e-2, (li, rel)
+
+
+def test_tc_pack_layers_matches_per_layer_packing(cuda):
+    import torch
+
+    specs = [(2, 16), (16, 16), (16, 16), (16, 1)]
+    Ws = [random_master(ci, co, 30 + i, cuda) for i, (ci, co) in enumerate(specs)]
+    one_f = [torch.zeros(capi.cnn_tc_weight_bytes(ci) // 2, dtype=torch.bfloat16, device=cuda)
+             for ci, _ in specs]
+    one_b = [torch.zeros(capi.cnn_tc_weight_bytes(co) // 2, dtype=torch.bfloat16, device=cuda)
+             for _, co in specs]
+    for (ci, co), W, f, b in zip(specs, Ws, one_f, one_b):
+        capi.cnn_tc_pack_weights(W, ci, co, f, b)
+    all_f = [torch.full_like(f, float("nan")) for f in one_f]
+    all_b = [None] + [torch.full_like(b, float("nan")) for b in one_b[1:]]
+    capi.cnn_tc_pack_layers(Ws, [s[0] for s in specs], [s[1] for s in specs], all_f, all_b)
+    torch.cuda.synchronize()
+    for i in range(4):
+        assert torch.equal(all_f[i], one_f[i])
+        if all_b[i] is not None:
+            assert torch.equal(all_b[i], one_b[i])
