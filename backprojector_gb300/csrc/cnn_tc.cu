@@ -90,7 +90,8 @@ constexpr uint32_t kConvLines = kConvLB + 3;          // y' lines staged per (x'
 constexpr uint32_t kConvBox = kConvLines * 32 * 16;   // bytes of one staged (x', plane) box
 constexpr uint32_t kConvStages = 4;
 constexpr uint32_t kConvAhead = 2;                    // a stage is refilled 2 blocks after use
-constexpr uint32_t kConvThreads = 160;
+constexpr uint32_t kConvThreads = 288;                // 8 epilogue warps + the producer
+constexpr uint32_t kConvProducer = 256;               // the producer / MMA thread
 constexpr uint32_t kConvN = 48;                       // dz x 16 output channels
 constexpr uint32_t kConvAccs = 4;                     // accumulators in flight
 constexpr uint32_t kConvAcc = 64;                     // columns per accumulator
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(kConvThreads)
         tmem_alloc(smem_addr(&taddr_s), kConvCols);
         tmem_relinquish();
     }
-    if (tid == 128) {
+    if (tid == kConvProducer) {
         for (uint32_t i = 0; i < kConvStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
             mbar_init(smem_addr(&empty[i]), 1);
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kConvThreads)
     tc_fence_after();
     const uint32_t taddr = taddr_s;
 
-    if (tid == 128) {
+    if (tid == kConvProducer) {
         // ---- producer (TMA) and MMA issue, one thread.  Stage of local block i:
         // i % kConvStages; the
         // stage of block it - kConvAhead (whose MMAs completed long ago) is refilled with
@@ -243,27 +244,38 @@ __global__ void __launch_bounds__(kConvThreads)
         }
         umma_commit(smem_addr(&drain));
         if (!mbar_wait(smem_addr(&drain), 0, kSpin)) fail(8);
-    } else if (tid < 128) {
-        // ---- epilogue: one voxel per thread (warp = line, lane = z)
-        uint32_t it = 0;
-        for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
+    } else if (warp < 8) {
+        // ---- epilogue: two groups of 4 warps take alternate blocks; in a group, warp q
+        // reads tensor-memory lanes 32 q.. (line q of the block), lane = z: one voxel each
+        const uint32_t grp = warp >> 2, q = warp & 3;
+        uint32_t it = grp;
+        for (uint64_t b = blockIdx.x + (uint64_t)grp * gridDim.x; b < a.nblocks;
+             b += 2ull * gridDim.x, it += 2) {
             const uint32_t ab = it % kConvAccs;
+            uint32_t s, x, y0;
+            conv_block((uint32_t)b, a.in, s, x, y0);
+            const uint32_t y = y0 + q, z = lane;
+            uint4 mk[2] = {make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+            if (a.mask) {  // the ReLU mask is known before the accumulator: fetch it first
+#pragma unroll
+                for (uint32_t h = 0; h < 2; h++)
+                    if (h < a.out.npl)
+                        mk[h] = *reinterpret_cast<const uint4 *>(
+                            a.mask + a.mk.row(s, x + 1, y + 1, h, z + a.mk.zp) * 16);
+            }
             if (!mbar_wait(smem_addr(&acc_full[ab]), (it / kConvAccs) & 1, kSpin)) {
                 fail(16);
                 break;
             }
             tc_fence_after();
             float dm[16], d0[16], dp[16];
-            const uint32_t t = taddr + ((warp * 32u) << 16) + ab * kConvAcc;
+            const uint32_t t = taddr + ((q * 32u) << 16) + ab * kConvAcc;
             tmem_ld16(t, dm);
             tmem_ld16(t + 16, d0);
             tmem_ld16(t + 32, dp);
             tmem_ld_wait();
             tc_fence_before();
             mbar_arrive(smem_addr(&acc_empty[ab]));
-            uint32_t s, x, y0;
-            conv_block(b, a.in, s, x, y0);
-            const uint32_t y = y0 + warp, z = lane;
             float o[16];
 #pragma unroll
             for (int co = 0; co < 16; co++) {
@@ -290,8 +302,7 @@ __global__ void __launch_bounds__(kConvThreads)
                     if (h >= a.out.npl) break;
                     float *oh = o + 8 * h;
                     if (a.mask) {
-                        const uint4 m = *reinterpret_cast<const uint4 *>(
-                            a.mask + a.mk.row(s, x + 1, y + 1, h, z + a.mk.zp) * 16);
+                        const uint4 m = mk[h];
                         const uint32_t mw[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
@@ -677,7 +688,7 @@ __global__ void bce_lp_kernel(const float *__restrict__ logits, const uint8_t *_
 // ---- host -----------------------------------------------------------------------------
 bool lp_of(const uint32_t *dims, uint32_t batch, uint32_t channels, uint32_t zp, Lp *g) {
     if (!dims || !batch || !dims[0] || !dims[1] || dims[2] != kZLine || channels == 0 ||
-        channels > 16 || zp > 1 || dims[1] % kWgLB)
+        channels > 16 || zp > 1 || dims[1] % 8)
         return false;
     g->n0 = dims[0];
     g->n1 = dims[1];

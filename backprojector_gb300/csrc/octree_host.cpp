@@ -37,7 +37,13 @@ struct bpgb_octree_s {
     float p_lo = 0.5f, logit_lo = 0.0f;
     bpgb_plan coarse_plan = nullptr, sparse_plan = nullptr;
     std::vector<Layer> layers;
-    std::vector<void *> wt;  // packed BF16 weights per layer
+    std::vector<void *> wt;  // packed BF16 weights per layer (mma.sync kernels)
+    // tensor-core path (coarse grids of 32-voxel z-lines): FP32 masters (bias rows), the
+    // tcgen05 weight images and the line-planes activations (padding rows zero)
+    bool tc = false;
+    std::vector<float *> master;
+    std::vector<void *> wtc;
+    void *Xl = nullptr, *Yl[3] = {nullptr, nullptr, nullptr};
     void *rows = nullptr;    // FP16 rows (FP16 mode)
     float *absmax = nullptr, *coarse_vol = nullptr, *logits = nullptr, *feat = nullptr;
     void *X = nullptr, *Y[3] = {nullptr, nullptr, nullptr};
@@ -54,6 +60,10 @@ void octree_free(bpgb_octree_s *o) {
     if (o->coarse_plan) bpgb_plan_destroy(o->coarse_plan);
     if (o->sparse_plan) bpgb_plan_destroy(o->sparse_plan);
     for (void *p : o->wt) cudaFree(p);
+    for (float *p : o->master) cudaFree(p);
+    for (void *p : o->wtc) cudaFree(p);
+    cudaFree(o->Xl);
+    for (void *p : o->Yl) cudaFree(p);
     cudaFree(o->rows);
     cudaFree(o->absmax);
     cudaFree(o->coarse_vol);
@@ -156,6 +166,7 @@ int bpgb_octree_create(bpgb_octree *out, const bpgb_pair *pairs, uint64_t num_pa
     // weights
     const uint64_t nc = (uint64_t)oc->coarse[0] * oc->coarse[1] * oc->coarse[2];
     cudaError_t e = cudaSuccess;
+    oc->tc = oc->coarse[2] == 32 && oc->coarse[1] % 8 == 0;
     for (size_t li = 0; li < oc->layers.size(); li++) {
         const Layer &L = oc->layers[li];
         const std::string key = "w" + std::to_string(li);
@@ -175,12 +186,35 @@ int bpgb_octree_create(bpgb_octree *out, const bpgb_pair *pairs, uint64_t num_pa
         if (d_t) oc->wt.push_back(d_t);
         if (e == cudaSuccess) {
             st = bpgb_cnn_pack_weights(d_m, L.cin, L.cout, L.np, d_t, 0, nullptr, nullptr);
-            if (st == 0) e = cudaDeviceSynchronize();
+            if (st == 0 && oc->tc) {
+                void *d_tc = nullptr;
+                const uint64_t tb = bpgb_cnn_tc_weight_bytes(L.cin);
+                e = cudaMalloc(&d_tc, tb);
+                if (d_tc) oc->wtc.push_back(d_tc);
+                if (e == cudaSuccess) st = bpgb_cnn_tc_pack_weights(d_m, L.cin, L.cout, d_tc, nullptr, nullptr);
+                oc->scratch += tb + m.size() * sizeof(float);
+            }
+            if (st == 0 && e == cudaSuccess) e = cudaDeviceSynchronize();
         }
-        cudaFree(d_m);
+        if (oc->tc && d_m)
+            oc->master.push_back(d_m);  // its bias row feeds the tensor-core epilogue
+        else
+            cudaFree(d_m);
         if (e != cudaSuccess) return fail(cuda_error(e, "octree weights"));
         if (st) return fail(st);
         oc->scratch += (uint64_t)L.np * kp * 2;
+    }
+    if (oc->tc) {
+        const uint64_t xb = bpgb_cnn_lp_bytes(oc->in_channels, 0, oc->coarse, 1);
+        const uint64_t yb = bpgb_cnn_lp_bytes(16, 0, oc->coarse, 1);
+        e = cudaMalloc(&oc->Xl, xb);
+        if (e == cudaSuccess) e = cudaMemset(oc->Xl, 0, xb);
+        for (int k = 0; k < 3 && e == cudaSuccess; k++) {
+            e = cudaMalloc(&oc->Yl[k], yb);
+            if (e == cudaSuccess) e = cudaMemset(oc->Yl[k], 0, yb);
+        }
+        if (e != cudaSuccess) return fail(cuda_error(e, "octree line-planes buffers"));
+        oc->scratch += xb + 3 * yb;
     }
     // buffers
     if (o.h_dtype == BPGB_DTYPE_F16) {
@@ -228,7 +262,23 @@ int bpgb_octree_reconstruct(bpgb_octree oc, const float *d_H, float *d_volume, v
     if (st) return st;
     const void *in = oc->X;
     uint32_t xs = oc->in_channels;
-    for (size_t li = 0; li < oc->layers.size(); li++) {
+    if (oc->tc) {
+        // tcgen05 kernels on line-planes tensors
+        if ((st = bpgb_cnn_lp_pack(oc->X, oc->in_channels, oc->in_channels, oc->coarse, 1, 0, oc->Xl, s)))
+            return st;
+        in = oc->Xl;
+        for (size_t li = 0; li < oc->layers.size(); li++) {
+            const Layer &L = oc->layers[li];
+            const bool last = li + 1 == oc->layers.size();
+            st = bpgb_cnn_tc_conv3d(in, L.cin, 0, oc->coarse, 1, oc->wtc[li],
+                                    oc->master[li] + 27 * L.cin * L.cout, L.cout, L.relu ? 1 : 0,
+                                    nullptr, last ? nullptr : oc->Yl[li], 0,
+                                    last ? oc->logits : nullptr, s);
+            if (st) return st;
+            if (!last) in = oc->Yl[li];
+        }
+    }
+    for (size_t li = 0; li < oc->layers.size() && !oc->tc; li++) {
         const Layer &L = oc->layers[li];
         const bool last = li + 1 == oc->layers.size();
         st = bpgb_cnn_conv3d(in, L.cin, xs, oc->coarse, 1, oc->wt[li], L.np, L.relu ? 1 : 0,

@@ -176,8 +176,35 @@ class OccupancyCNN:
             capi.cnn_features(coarse, dims, batch, X, scr, stream)
         return X
 
-    def forward(self, X0, dims, batch: int, logits=None, stream=None):
-        """logits (FP32 [batch * prod(dims)]) of input features X0 (features())."""
+    def forward(self, X0, dims, batch: int, logits=None, stream=None, tc: bool | None = None):
+        """logits (FP32 [batch * prod(dims)]) of input features X0 (features()): on the
+        tcgen05 kernels when the volume allows it (tc=None), else on the mma.sync kernels."""
+        if tc is None:
+            tc = self.tc_supported(dims)
+        if tc:
+            if logits is None:
+                logits = self._buf("Z", (batch * int(np.prod(dims)),), self.torch.float32)
+            self._forward_tc(X0, dims, batch, logits, stream)
+            return logits
+        return self._forward_mma(X0, dims, batch, logits, stream)
+
+    def _forward_tc(self, X0, dims, batch, logits, stream):
+        """Forward pass on line-planes tensors; returns (layer inputs, activations)."""
+        ci = self.in_channels
+        X0l = self._lp(f"X0l_{batch}", ci, 0, dims, batch)
+        Yl = [self._lp(f"Y{i}l_{batch}", 16, 0, dims, batch) for i in (1, 2, 3)]
+        capi.cnn_lp_pack(X0, ci, ci, dims, batch, 0, X0l, stream)
+        ins = [X0l] + Yl
+        for li, (cin, cout, relu) in enumerate(self.layers):
+            if li < 3:
+                capi.cnn_tc_conv3d(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout,
+                                   relu, d_Y=Yl[li], stream=stream)
+            else:
+                capi.cnn_tc_conv3d(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout,
+                                   False, d_Yf=logits, stream=stream)
+        return ins, Yl
+
+    def _forward_mma(self, X0, dims, batch, logits, stream):
         torch = self.torch
         if self._mma_stale:
             self.pack_mma(stream)
@@ -223,8 +250,6 @@ class OccupancyCNN:
         torch = self.torch
         V = batch * int(np.prod(dims))
         ci = self.in_channels
-        X0l = self._lp("X0l", ci, 0, dims, batch)
-        Yl = [self._lp(f"Y{i}l", 16, 0, dims, batch) for i in (1, 2, 3)]
         dZl = self._lp("dZl", 1, 1, dims, batch)
         dYl = [self._lp(f"dY{i}l", 16, 1, dims, batch) for i in (1, 2, 3)]
         logits = self._buf("Z", (V,), torch.float32)
@@ -234,16 +259,7 @@ class OccupancyCNN:
                    capi.cnn_tc_wgrad_scratch_bytes(ci, dims, batch))
         scr = self._buf("tc_scratch", (nscr // 4,), torch.float32)
         conv, wgrad = capi.cnn_tc_conv3d, capi.cnn_tc_conv3d_wgrad
-        capi.cnn_lp_pack(X0, ci, ci, dims, batch, 0, X0l, stream)
-        # forward
-        ins = [X0l] + Yl
-        for li, (cin, cout, relu) in enumerate(self.layers):
-            if li < 3:
-                conv(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout, relu,
-                     d_Y=Yl[li], stream=stream)
-            else:
-                conv(ins[li], cin, 0, dims, batch, self.Wtc[li], self.bias(li), cout, False,
-                     d_Yf=logits, stream=stream)
+        ins, Yl = self._forward_tc(X0, dims, batch, logits, stream)
         capi.cnn_tc_bce_grad(logits, labels, dims, batch, pos_weight, 1.0 / V, dZl, loss, stream)
         # backward: weight gradient of layer li, then the input gradient (masked by the
         # ReLU of the layer below)
@@ -268,7 +284,7 @@ class OccupancyCNN:
     def _train_step_mma(self, X0, labels, dims, batch, lr, pos_weight, stream):
         torch = self.torch
         V = batch * int(np.prod(dims))
-        logits = self.forward(X0, dims, batch, stream=stream)
+        logits = self.forward(X0, dims, batch, stream=stream, tc=False)
         Y1, Y2, Y3 = self._bufs["Y1"], self._bufs["Y2"], self._bufs["Y3"]
         dZ = self._buf("dZ", (V, 8), torch.bfloat16)
         loss = self._buf("loss", (V,), torch.float32)
