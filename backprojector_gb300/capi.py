@@ -133,6 +133,7 @@ SIGNATURES: dict[str, tuple] = {
     "bpgb_plan_select_tiles_topk": (C.c_int, [_P, _P, _U32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "bpgb_diag_mufu_rates": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "bpgb_diag_umma_probe": (C.c_int, [_P, C.c_uint32, _U32, _F, _U32]),
+    "bpgb_diag_umma_issue_rates": (C.c_int, [C.POINTER(C.c_double), C.c_int]),
     "bpgb_set_dropin_algo": (C.c_int, [C.c_int]),
     "bpgb_get_dropin_algo": (C.c_int, []),
     "bpgb_plan_get_tables": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
@@ -308,6 +309,14 @@ def mufu_rates() -> dict:
     r = (C.c_double * 6)()
     check(lib().bpgb_diag_mufu_rates(r, 6), "bpgb_diag_mufu_rates")
     return dict(zip(("rsqrt_8_chains", "rsqrt_16_chains", "ex2", "sqrt", "rcp", "sin"), list(r)))
+
+
+def umma_issue_rates() -> dict:
+    """Cycles per tcgen05.mma by shape, one issuing thread per SM (bpgb_diag_umma_issue_rates)."""
+    r = (C.c_double * 6)()
+    check(lib().bpgb_diag_umma_issue_rates(r, 6), "bpgb_diag_umma_issue_rates")
+    keys = ("m128_n48_mn", "m64_n48_mn", "m128_n48_k", "m128_n96_k", "m128_n128_k", "m128_n256_k")
+    return dict(zip(keys, list(r)))
 
 
 def umma_probe(image: np.ndarray, params, ncols: int):

@@ -151,6 +151,7 @@ double per_sm_rate(const std::vector<ProbeOut> &h, int sms, double ops_per_cta) 
 constexpr uint32_t kUmmaImage = 48 * 1024;
 constexpr uint32_t kUmmaSmem = 96 * 1024;
 constexpr uint32_t kUmmaCols = 256;
+constexpr uint32_t kUmmaRateSmem = 64 * 1024;
 
 struct UmmaProbeArgs {
     uint32_t a_off, a_lbo, a_sbo, a_kstep;
@@ -213,6 +214,83 @@ __global__ void __launch_bounds__(128) umma_probe_kernel(const uint4 *__restrict
         tc_fence_after();
         tmem_dealloc(taddr, kUmmaCols);
     }
+}
+
+// ---- tcgen05 issue rate -----------------------------------------------------------------
+// One thread per CTA (one CTA per SM) issues `reps` back-to-back MMAs of one shape over
+// NACC independent accumulators, operands zero in shared memory; clock64 around the
+// issue loop and the commit wait gives cycles per MMA.
+template <uint32_t M, uint32_t N, bool MN, uint32_t NACC>
+__global__ void __launch_bounds__(128) umma_rate_kernel(uint32_t reps, unsigned long long *out,
+                                                        uint32_t *status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t taddr_s;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    for (uint32_t i = tid; i < kUmmaRateSmem / 16; i += 128)
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0, 0, 0, 0);
+    fence_async_smem();
+    if (warp == 0) {
+        tmem_alloc(smem_addr(&taddr_s), 512);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        mbar_init(smem_addr(&bar), 1);
+        mbar_fence_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t taddr = taddr_s;
+    if (tid == 0) {
+        const uint32_t base = smem_addr(smem);
+        // A at 0 and B at 32 KB; the widest reading (16 / 32 core matrices) stays below 48 KB
+        const uint64_t ad = MN ? umma_smem_desc(base, 128, 512) : umma_smem_desc(base, 2048, 128);
+        const uint64_t bd = MN ? umma_smem_desc(base + 32768, 128, 512)
+                               : umma_smem_desc(base + 32768, 4096, 128);
+        constexpr uint32_t idesc = umma_idesc_bf16(M, N, MN, MN);
+#pragma unroll
+        for (uint32_t u = 0; u < NACC; u++) umma_bf16(taddr + u * N, ad, bd, idesc, 0);
+        const unsigned long long t0 = clock64();
+        for (uint32_t r = 0; r < reps; r += NACC) {
+#pragma unroll
+            for (uint32_t u = 0; u < NACC; u++) umma_bf16(taddr + u * N, ad, bd, idesc, 1);
+        }
+        umma_commit(smem_addr(&bar));
+        const bool ok = mbar_wait(smem_addr(&bar), 0, 1u << 24);
+        const unsigned long long t1 = clock64();
+        if (!ok) atomicOr(status, 1u);
+        out[blockIdx.x] = t1 - t0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(taddr, 512);
+    }
+}
+
+template <uint32_t M, uint32_t N, bool MN, uint32_t NACC>
+int umma_rate(int sms, unsigned long long *d, uint32_t *st, double *cycles) {
+    const uint32_t reps = 2048;
+    cudaError_t e = cudaFuncSetAttribute(umma_rate_kernel<M, N, MN, NACC>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kUmmaRateSmem);
+    for (int rep = 0; rep < 2 && e == cudaSuccess; rep++) {  // the first launch warms up
+        umma_rate_kernel<M, N, MN, NACC><<<sms, 128, kUmmaRateSmem>>>(reps, d, st);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
+    std::vector<unsigned long long> h(sms);
+    uint32_t hs = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(h.data(), d, sms * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&hs, st, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "umma rate probe");
+    if (hs) return set_error(BPGB_ERR_TIMEOUT, "umma rate probe: commit wait ran out");
+    double sum = 0.0;
+    for (unsigned long long c : h) sum += (double)c;
+    *cycles = sum / sms / reps;
+    return BPGB_OK;
 }
 
 }  // namespace
@@ -348,4 +426,32 @@ extern "C" int bpgb_diag_pipe_rates(double *rates) {
     }
     cudaFree(d);
     return BPGB_OK;
+}
+
+// Cycles per tcgen05.mma (BF16, K = 16) issued back to back by one thread per SM over
+// independent accumulators: [0] M128 N48 MN-major, [1] M64 N48 MN-major, [2] M128 N48
+// K-major, [3] M128 N96 K-major, [4] M128 N128 K-major, [5] M128 N256 K-major.
+extern "C" int bpgb_diag_umma_issue_rates(double *cycles, int n) {
+    clear_error();
+    if (!cycles || n < 1) return set_error(BPGB_ERR_INVALID_ARGUMENT, "cycles is null or n < 1");
+    int sms = 0;
+    int st = require_device(&sms);
+    if (st) return st;
+    unsigned long long *d = nullptr;
+    uint32_t *ds = nullptr;
+    cudaError_t e = cudaMalloc(&d, sms * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ds, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ds, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        cudaFree(ds);
+        return cuda_error(e, "umma rate probe");
+    }
+    int (*run[6])(int, unsigned long long *, uint32_t *, double *) = {
+        umma_rate<128, 48, true, 8>,  umma_rate<64, 48, true, 8>,   umma_rate<128, 48, false, 8>,
+        umma_rate<128, 96, false, 4>, umma_rate<128, 128, false, 2>, umma_rate<128, 256, false, 2>};
+    for (int i = 0; i < 6 && i < n && !st; i++) st = run[i](sms, d, ds, &cycles[i]);
+    cudaFree(d);
+    cudaFree(ds);
+    return st;
 }

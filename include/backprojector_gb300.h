@@ -556,6 +556,11 @@ int bpgb_diag_mufu_rates(double *rates, int n);
  * commit wait ran out.  Pins the descriptor and accumulator layouts the CNN kernels use. */
 int bpgb_diag_umma_probe(const void *h_image, uint32_t image_bytes, const uint32_t *params,
                          float *h_out, uint32_t *h_status);
+/* Cycles per tcgen05.mma (BF16, K = 16) issued back to back by one thread on each SM over
+ * independent accumulators, operands in shared memory: cycles[0] M128 N48 MN-major, [1]
+ * M64 N48 MN-major, [2] M128 N48 K-major, [3] M128 N96, [4] M128 N128, [5] M128 N256
+ * (K-major) -- the first n of them.  The issue floor of the CNN kernels' small MMAs. */
+int bpgb_diag_umma_issue_rates(double *cycles, int n);
 
 /* ---- phasor pulse --------------------------------------------------------
  * d_out[r, t] = sum_k d_H[r, t + k - K/2] * (cos_k, sin_k), read index in (0, T), with

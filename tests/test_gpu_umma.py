@@ -106,3 +106,12 @@ def test_umma_layouts(cuda, name):
     assert found, f"{name}: no stride assignment reproduces A @ B^T"
     for swap_a, swap_b, lanes in found:
         print(f"[{name}] MATCH swap_a={swap_a} swap_b={swap_b} lanes={lanes}")
+
+
+def test_umma_issue_rates(cuda):
+    """The MMA issue floor: a small MMA costs a fixed number of cycles, a full-width one
+    (M128 N256) runs at the dense BF16 rate (M N K / 4096 MACs per clock = 128 cycles)."""
+    r = capi.umma_issue_rates()
+    print("\ncycles per tcgen05.mma:", {k: round(v, 1) for k, v in r.items()})
+    assert all(v > 0 for v in r.values())
+    assert r["m128_n256_k"] >= r["m128_n48_k"]
