@@ -89,9 +89,9 @@ constexpr uint32_t kConvLB = 4;                       // output lines per block 
 constexpr uint32_t kConvLines = kConvLB + 3;          // y' lines staged per (x', plane), 1 spare
 constexpr uint32_t kConvBox = kConvLines * 32 * 16;   // bytes of one staged (x', plane) box
 constexpr uint32_t kConvStages = 4;
-constexpr uint32_t kConvAhead = 2;                    // a stage is refilled 2 blocks after use
-constexpr uint32_t kConvThreads = 288;                // 8 epilogue warps + the producer
-constexpr uint32_t kConvProducer = 256;               // the producer / MMA thread
+constexpr uint32_t kConvThreads = 320;                // 8 epilogue warps, MMA warp, TMA warp
+constexpr uint32_t kConvMma = 256;                    // the MMA-issuing thread
+constexpr uint32_t kConvTma = 288;                    // the TMA-issuing thread
 constexpr uint32_t kConvN = 48;                       // dz x 16 output channels
 constexpr uint32_t kConvAccs = 4;                     // accumulators in flight
 constexpr uint32_t kConvAcc = 64;                     // columns per accumulator
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kConvThreads)
         tmem_alloc(smem_addr(&taddr_s), kConvCols);
         tmem_relinquish();
     }
-    if (tid == kConvProducer) {
+    if (tid == kConvMma) {
         for (uint32_t i = 0; i < kConvStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
             mbar_init(smem_addr(&empty[i]), 1);
@@ -170,32 +170,35 @@ __global__ void __launch_bounds__(kConvThreads)
     tc_fence_after();
     const uint32_t taddr = taddr_s;
 
-    if (tid == kConvProducer) {
-        // ---- producer (TMA) and MMA issue, one thread.  Stage of local block i:
-        // i % kConvStages; the
-        // stage of block it - kConvAhead (whose MMAs completed long ago) is refilled with
-        // block it - kConvAhead + kConvStages right after block it's MMAs are issued.
-        auto copy = [&](uint32_t st, uint32_t b, bool weights) {
-            uint32_t s, x, y0;
-            conv_block(b, a.in, s, x, y0);
-            const uint32_t bar = smem_addr(&full[st]);
-            mbar_expect_tx(bar, S::kStage + (weights ? S::kWBytes : 0u));
-            if (weights) bulk_g2s(smem_addr(w_s), a.W, S::kWBytes, bar);
-            const uint32_t dst = smem_addr(stage_s + st * S::kStage);
-            const int32_t xg = (int32_t)(s * (a.in.n0 + 2) + x);
-            for (uint32_t dx = 0; dx < 3; dx++)
-                for (uint32_t h = 0; h < NPL; h++)
-                    tma_load_4d(dst + (dx * NPL + h) * kConvBox, &tmap, (int32_t)(a.in.zp * 8),
-                                (int32_t)h, (int32_t)y0, xg + (int32_t)dx, bar);
-            mbar_arrive(bar);
-        };
+    auto copy = [&](uint32_t st, uint32_t b, bool weights) {
+        uint32_t s, x, y0;
+        conv_block(b, a.in, s, x, y0);
+        const uint32_t bar = smem_addr(&full[st]);
+        mbar_expect_tx(bar, S::kStage + (weights ? S::kWBytes : 0u));
+        if (weights) bulk_g2s(smem_addr(w_s), a.W, S::kWBytes, bar);
+        const uint32_t dst = smem_addr(stage_s + st * S::kStage);
+        const int32_t xg = (int32_t)(s * (a.in.n0 + 2) + x);
+        // one box: 3 x' x the planes x 7 lines x 32 voxels, landing [dx][plane][line][z]
+        tma_load_4d(dst, &tmap, (int32_t)(a.in.zp * 8), (int32_t)y0, 0, xg, bar);
+        mbar_arrive(bar);
+    };
+    if (tid == kConvTma) {
+        // ---- TMA producer: the stage of local block i is i % kConvStages, refilled as
+        // soon as the MMAs of block i - kConvStages have completed
+        uint32_t it = 0;
+        for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
+            const uint32_t st = it % kConvStages;
+            if (it >= kConvStages &&
+                !mbar_wait(smem_addr(&empty[st]), ((it / kConvStages) - 1) & 1, kSpin)) {
+                fail(4);
+                break;
+            }
+            copy(st, b, it == 0);
+        }
+    } else if (tid == kConvMma) {
+        // ---- MMA issue
         const uint32_t idesc = umma_idesc_bf16(128, kConvN, false, false);
         const uint32_t wbase = smem_addr(w_s);
-        for (uint32_t i = 0; i < kConvStages; i++) {
-            const uint64_t b = blockIdx.x + (uint64_t)i * gridDim.x;
-            if (b >= a.nblocks) break;
-            copy(i, (uint32_t)b, i == 0);
-        }
         uint32_t it = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kConvStages, ab = it % kConvAccs;
@@ -229,18 +232,6 @@ __global__ void __launch_bounds__(kConvThreads)
             }
             umma_commit(smem_addr(&empty[st]));
             umma_commit(smem_addr(&acc_full[ab]));
-            if (it >= kConvAhead) {
-                const uint32_t old = it - kConvAhead;
-                const uint64_t pb = blockIdx.x + (uint64_t)(old + kConvStages) * gridDim.x;
-                if (pb < a.nblocks) {
-                    const uint32_t ps = old % kConvStages;
-                    if (!mbar_wait(smem_addr(&empty[ps]), (old / kConvStages) & 1, kSpin)) {
-                        fail(4);
-                        break;
-                    }
-                    copy(ps, (uint32_t)pb, false);
-                }
-            }
         }
         umma_commit(smem_addr(&drain));
         if (!mbar_wait(smem_addr(&drain), 0, kSpin)) fail(8);
@@ -328,7 +319,9 @@ __global__ void __launch_bounds__(kConvThreads)
 // ---- weight gradient ----------------------------------------------------------------
 constexpr uint32_t kWgLB = 4;       // output lines per block
 constexpr uint32_t kWgStages = 3;
-constexpr uint32_t kWgThreads = 160;
+constexpr uint32_t kWgThreads = 192;  // 4 epilogue warps, the MMA warp, the TMA warp
+constexpr uint32_t kWgMma = 128;      // the MMA-issuing thread
+constexpr uint32_t kWgTma = 160;      // the TMA-issuing thread
 constexpr uint32_t kWgCols = 128;   // M = 128 and M = 64 accumulators (48 columns) + bias (16)
 constexpr uint32_t kWgAcc64 = 48;   // column of the M = 64 accumulator
 constexpr uint32_t kWgBias = 96;    // column of the bias accumulator
@@ -338,6 +331,7 @@ constexpr uint32_t kWgBLine = 3 * 2 * 512;  // per output line: (k, plane) block
 struct WgradArgs {
     Lp xin;            // activation (zp 0), read through its tensor map
     Lp dy;             // gradient (zp 1), read through its tensor map
+    int dy_one_box;    // the gradient map is the 5-D one-box form (two planes)
     uint32_t cin, cout, kp;
     float *partial;    // [gridDim.x][kp][16]
     uint32_t nblocks;
@@ -403,7 +397,7 @@ __global__ void __launch_bounds__(kWgThreads)
         tmem_alloc(smem_addr(&taddr_s), kWgCols);
         tmem_relinquish();
     }
-    if (tid == 128) {
+    if (tid == kWgMma) {
         for (uint32_t i = 0; i < kWgStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
             mbar_init(smem_addr(&empty[i]), 1);
@@ -417,31 +411,42 @@ __global__ void __launch_bounds__(kWgThreads)
     const uint32_t taddr = taddr_s;
     const bool any = blockIdx.x < a.nblocks;
 
-    if (tid == 128) {
-        // ---- producer (TMA) and MMA issue, one thread
-        auto copy = [&](uint32_t st, uint32_t b) {
-            uint32_t s, x, y0;
-            wg_block(b, a.dy, s, x, y0);
-            const uint32_t bar = smem_addr(&full[st]);
-            mbar_expect_tx(bar, S::kXBytes + kWgLB * 3 * a.dy.npl * 512);
-            const uint32_t dst = smem_addr(stage_s + st * S::kStage);
-            const int32_t xg = (int32_t)(s * (a.dy.n0 + 2) + x);
-            tma_load_4d(dst, &xmap, 0, 0, xg, (int32_t)y0, bar);
+    auto copy = [&](uint32_t st, uint32_t b) {
+        uint32_t s, x, y0;
+        wg_block(b, a.dy, s, x, y0);
+        const uint32_t bar = smem_addr(&full[st]);
+        mbar_expect_tx(bar, S::kXBytes + kWgLB * 3 * a.dy.npl * 512);
+        const uint32_t dst = smem_addr(stage_s + st * S::kStage);
+        const int32_t xg = (int32_t)(s * (a.dy.n0 + 2) + x);
+        tma_load_4d(dst, &xmap, 0, 0, xg, (int32_t)y0, bar);
+        if (a.dy_one_box)  // [line][k][plane][32 rows] in one box (k = a 16-byte shift)
+            tma_load_5d(dst + S::kXBytes, &dymap, 0, 0, 0, (int32_t)(y0 + 1), xg + 1, bar);
+        else
             for (uint32_t j = 0; j < kWgLB; j++)
                 for (uint32_t k = 0; k < 3; k++)
                     tma_load_4d(dst + S::kXBytes + j * kWgBLine + k * 1024, &dymap,
                                 (int32_t)(k * 8), 0, (int32_t)(y0 + 1 + j), xg + 1, bar);
-            mbar_arrive(bar);
-        };
+        mbar_arrive(bar);
+    };
+    if (tid == kWgTma) {
+        // ---- TMA producer: the stage of local block i is i % kWgStages, refilled as soon
+        // as the MMAs of block i - kWgStages have completed
+        uint32_t it = 0;
+        for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
+            const uint32_t st = it % kWgStages;
+            if (it >= kWgStages &&
+                !mbar_wait(smem_addr(&empty[st]), ((it / kWgStages) - 1) & 1, kSpin)) {
+                fail(64);
+                break;
+            }
+            copy(st, b);
+        }
+    } else if (tid == kWgMma) {
+        // ---- MMA issue
         const uint32_t idesc128 = umma_idesc_bf16(128, 48, true, true);
         const uint32_t idesc64 = umma_idesc_bf16(64, 48, true, true);
         const uint32_t idesc16 = umma_idesc_bf16(64, 16, true, true);
         const uint64_t ones_d = umma_smem_desc(smem_addr(ones), 128, 256);
-        for (uint32_t i = 0; i < kWgStages; i++) {
-            const uint64_t b = blockIdx.x + (uint64_t)i * gridDim.x;
-            if (b >= a.nblocks) break;
-            copy(i, (uint32_t)b);
-        }
         uint32_t it = 0, acc = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kWgStages;
@@ -454,7 +459,7 @@ __global__ void __launch_bounds__(kWgThreads)
             // descriptors of line 0, K step 0; later lines / steps add to the start field
             const uint64_t ad0 = umma_smem_desc(xs, 128, 512);
             const uint64_t bd0 = umma_smem_desc(xs + S::kXBytes, 128, 512);
-#pragma unroll 1
+#pragma unroll
             for (uint32_t j = 0; j < kWgLB; j++) {
 #pragma unroll
                 for (uint32_t ks = 0; ks < 2; ks++) {
@@ -467,19 +472,6 @@ __global__ void __launch_bounds__(kWgThreads)
                 }
             }
             umma_commit(smem_addr(&empty[st]));
-            // refill the previous block's stage with the block kWgStages after it
-            if (it >= 1) {
-                const uint32_t old = it - 1;
-                const uint64_t pb = blockIdx.x + (uint64_t)(old + kWgStages) * gridDim.x;
-                if (pb < a.nblocks) {
-                    const uint32_t ps = old % kWgStages;
-                    if (!mbar_wait(smem_addr(&empty[ps]), (old / kWgStages) & 1, kSpin)) {
-                        fail(64);
-                        break;
-                    }
-                    copy(ps, (uint32_t)pb);
-                }
-            }
         }
         umma_commit(smem_addr(&done));
     } else if (tid < 128) {
@@ -540,24 +532,42 @@ __global__ void __launch_bounds__(kWgThreads)
 }
 
 // dW[k][n] = sum over CTAs of partial[p][k][n] (k <= 27 cin), 0 on the padding rows.
-// One CTA per row k: thread (p0, n) sums p = p0, p0 + 16, ... in order, then a fixed tree
-// over p0 (deterministic).
+// One CTA per row k: thread (p0, q) sums the float4 of channels 4q .. 4q + 3 over
+// p = p0, p0 + 64, ... in order, then a fixed tree over p0 (deterministic).
 __global__ void __launch_bounds__(256) wgrad_tc_reduce_kernel(const float *__restrict__ partial,
                                                               uint32_t parts, uint32_t kp,
                                                               uint32_t cin, uint32_t cout,
                                                               float *__restrict__ dW) {
-    __shared__ float red[16][17];
-    const uint32_t k = blockIdx.x, n = threadIdx.x % 16, p0 = threadIdx.x / 16;
-    float s = 0.0f;
+    __shared__ float4 red[64][4];
+    const uint32_t k = blockIdx.x, q = threadIdx.x % 4, p0 = threadIdx.x / 4;
+    float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (k <= 27 * cin)
-        for (uint32_t p = p0; p < parts; p += 16) s += partial[((uint64_t)p * kp + k) * 16 + n];
-    red[p0][n] = s;
+        for (uint32_t p = p0; p < parts; p += 64) {
+            const float4 v =
+                reinterpret_cast<const float4 *>(partial + ((uint64_t)p * kp + k) * 16)[q];
+            s.x += v.x;
+            s.y += v.y;
+            s.z += v.z;
+            s.w += v.w;
+        }
+    red[p0][q] = s;
     __syncthreads();
-    for (uint32_t w = 8; w > 0; w >>= 1) {
-        if (p0 < w) red[p0][n] += red[p0 + w][n];
+    for (uint32_t w = 32; w > 0; w >>= 1) {
+        if (p0 < w) {
+            const float4 o = red[p0 + w][q];
+            float4 &r = red[p0][q];
+            r.x += o.x;
+            r.y += o.y;
+            r.z += o.z;
+            r.w += o.w;
+        }
         __syncthreads();
     }
-    if (p0 == 0 && n < cout) dW[(uint64_t)k * cout + n] = red[0][n];
+    if (threadIdx.x < 16 && threadIdx.x < cout) {
+        const float4 r = red[0][threadIdx.x / 4];
+        const uint32_t c = threadIdx.x % 4;
+        dW[(uint64_t)k * cout + threadIdx.x] = c == 0 ? r.x : c == 1 ? r.y : c == 2 ? r.z : r.w;
+    }
 }
 
 // ---- layout conversion, weights, loss ----------------------------------------------------
@@ -834,11 +844,12 @@ int bpgb_cnn_tc_conv3d(const void *d_X, uint32_t in_channels, uint32_t in_zpad,
     if (!tensor_map_encoder()) return set_error(BPGB_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
     // the input as [x' (with sample)][y'][plane][z' x 8 channels]: boxes of 7 lines x the
     // line's 32 voxels (256 elements, 512 B contiguous) of one plane
+    // (dimension 1 is y', dimension 2 the plane: one box lands [x'][plane][y'][z])
     const Lp &g = a.in;
-    const cuuint64_t gdims[4] = {g.L() * 8ull, g.npl, g.n1 + 2ull, (cuuint64_t)batch * (g.n0 + 2)};
-    const cuuint64_t gstr[3] = {g.L() * 16ull, (cuuint64_t)g.line_rows() * 16,
+    const cuuint64_t gdims[4] = {g.L() * 8ull, g.n1 + 2ull, g.npl, (cuuint64_t)batch * (g.n0 + 2)};
+    const cuuint64_t gstr[3] = {(cuuint64_t)g.line_rows() * 16, g.L() * 16ull,
                                 (g.n1 + 2ull) * g.line_rows() * 16};
-    const cuuint32_t box[4] = {256, 1, kConvLines, 1};
+    const cuuint32_t box[4] = {256, kConvLines, g.npl, 3};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     CUtensorMap map;
     CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
@@ -887,7 +898,8 @@ int bpgb_cnn_tc_conv3d_wgrad(const void *d_X, uint32_t in_channels, const void *
     clear_error();
     WgradArgs a{};
     if (!d_X || !d_dY || !d_dW || !d_scratch || !lp_of(dims, batch, in_channels, 0, &a.xin) ||
-        !lp_of(dims, batch, out_channels, 1, &a.dy) || !aligned16(d_X) || !aligned16(d_dY))
+        !lp_of(dims, batch, out_channels, 1, &a.dy) || !aligned16(d_X) || !aligned16(d_dY) ||
+        !aligned16(d_scratch))
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "bad tc_conv3d_wgrad arguments");
     if (scratch_bytes < bpgb_cnn_tc_wgrad_scratch_bytes(in_channels, dims, batch))
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "tc wgrad scratch too small");
@@ -909,11 +921,28 @@ int bpgb_cnn_tc_conv3d_wgrad(const void *d_X, uint32_t in_channels, const void *
                                 gx.npl == 2 ? WgShape<2>::kXL : WgShape<1>::kXL};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     CUtensorMap map, xmap;
-    CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
-                                      const_cast<void *>(d_dY), gdims, gstr, box, estr,
-                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = CUDA_ERROR_INVALID_VALUE;
+    if (g.npl == 2) {
+        // one box per block: [line 4][k 3][plane][32 rows], k a dimension of stride 16 B
+        // (the row shift of the three z taps; its windows overlap by design)
+        const cuuint64_t d5[5] = {256, 2, 3, g.n1 + 2ull, (cuuint64_t)batch * (g.n0 + 2)};
+        const cuuint64_t s5[4] = {g.L() * 16ull, 16, (cuuint64_t)g.line_rows() * 16,
+                                  (g.n1 + 2ull) * g.line_rows() * 16};
+        const cuuint32_t b5[5] = {256, 2, 3, kWgLB, 1};
+        const cuuint32_t e5[5] = {1, 1, 1, 1, 1};
+        r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5,
+                                 const_cast<void *>(d_dY), d5, s5, b5, e5,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        a.dy_one_box = r == CUDA_SUCCESS;
+    }
+    if (!a.dy_one_box)
+        r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                                 const_cast<void *>(d_dY), gdims, gstr, box, estr,
+                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r == CUDA_SUCCESS)
         r = tensor_map_encoder()(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
                                  const_cast<void *>(d_X), xdims, xstr, xbox, estr,
@@ -974,3 +1003,4 @@ int bpgb_cnn_tc_status(uint32_t *status, int reset) {
 }
 
 }  // extern "C"
+
