@@ -12,32 +12,34 @@
 // so every 3x3 neighbourhood in x and y is a fixed row offset.  Activations (inputs of
 // the forward convolutions) use zp = 0, gradients zp = 1.
 //
-// Convolution (conv_tc_kernel): per output z-line, for each of the 9 (dx, dy) taps one
-// tcgen05.mma with M = 64 (rows dz x 16 output channels, 48 used), N = 32 (the line's
-// voxels), K = 16 (input channels; for single-plane inputs K = 8 channels x 2 taps):
-//   D[dz, co][z] += sum_ci W[dx, dy, dz][ci][co] X[x + dx, y + dy, z][ci]
-// Both operands are K-major and read in place: A is the packed weight image, B the staged
-// input lines (8 voxels x 16 B core matrices along the line).  The z taps are folded
-// into M and recombined in the epilogue: Y[z] = D[dz=-1][z-1] + D[0][z] + D[+1][z+1]
-// (zero outside the line), then bias, ReLU or the ReLU mask of the backward pass.
+// Convolution (conv_tc_kernel): a block is 4 output z-lines of one (sample, x); for each
+// of the 9 (dx, dy) taps one tcgen05.mma with M = 128 (the block's voxels), N = 48 (3 z
+// taps x 16 output channels), K = 16 (input channels; for single-plane inputs 8 channels
+// x 2 taps):
+//   D[z][dz, co] += sum_ci X[x + dx, y + dy, z][ci] W[dx, dy, dz][ci][co]
+// Both operands are K-major and read in place: A the staged input lines (core matrices of
+// 8 voxels along a line), B the packed weight image.  The z taps are recombined in the
+// epilogue, where thread = voxel: Y[z] = D[z-1][-1] + D[z][0] + D[z+1][+1] by warp
+// shuffles (zero outside the line), then bias, ReLU or the ReLU mask of the backward pass.
 //
-// Weight gradient (wgrad_tc_kernel): for each output line and each (dx, dz), one
-// tcgen05.mma with M = 64 (rows dy'' x plane x 8 channels; dy'' = 0..2 used, 3 in range
-// but unused), N = 16 output channels, K = 16 voxels of the line, both operands MN-major
-// and read in place from the staged lines:
-//   D[dx, dz][dy'', ci][co] += sum_z X[x + dx, y + dy'' - 1, z][ci] dY[x, y, z - dz][co]
-// (z - dz reads the gradient's zero z-padding at the ends), plus one MMA with an all-ones
-// A for the bias gradient.  Each CTA accumulates its lines in tensor memory and writes
-// one partial [kp][16]; a second kernel sums the partials in CTA order.
+// Weight gradient (wgrad_tc_kernel): for each output line and each 16-voxel K step,
+// tcgen05.mma with both operands MN-major and read in place from TMA-staged lines: A = the
+// activation's (dy, dx, plane) core matrices (M = 128 + 64), B = the gradient line at its
+// three z shifts (N = 48):
+//   D[dy, dx, ci][dz, co] += sum_z X[x + dx, y + dy, z][ci] dY[x, y, z - dz][co]
+// (z - dz reads the gradient's zero z-padding at the ends).  The bias gradient is summed
+// from the staged gradient by the otherwise idle epilogue warps.  Each CTA accumulates its
+// lines in tensor memory and writes one partial [kp][16]; a second kernel sums the
+// partials in CTA order.
 //
 // Descriptor and accumulator layouts are the ones bpgb_diag_umma_probe pins: LBO = the
 // K-direction core-matrix stride and SBO = the M/N-direction stride for both K-major and
 // MN-major operands; with M = 64, row r of D is tensor-memory lane 32 (r / 16) + r % 16.
 //
-// Each CTA runs 4 epilogue warps and one producer/MMA warp (one elected thread issues the
-// bulk copies and the MMAs).  Every mbarrier wait is bounded; a wait that gives up sets
-// g_tc_status (read by bpgb_cnn_tc_status) and the CTA drains its MMAs before it frees
-// its tensor memory.
+// Each CTA runs one thread that issues the TMA copies, one that issues the MMAs and
+// commits them to mbarriers, and epilogue warps; stages and accumulators are rings.  Every
+// mbarrier wait is bounded; a wait that gives up sets g_tc_status (read by
+// bpgb_cnn_tc_status) and the CTA drains its MMAs before it frees its tensor memory.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -322,10 +324,8 @@ constexpr uint32_t kWgStages = 3;
 constexpr uint32_t kWgThreads = 192;  // 4 epilogue warps, the MMA warp, the TMA warp
 constexpr uint32_t kWgMma = 128;      // the MMA-issuing thread
 constexpr uint32_t kWgTma = 160;      // the TMA-issuing thread
-constexpr uint32_t kWgCols = 128;   // M = 128 and M = 64 accumulators (48 columns) + bias (16)
+constexpr uint32_t kWgCols = 128;   // M = 128 and M = 64 accumulators (48 columns each)
 constexpr uint32_t kWgAcc64 = 48;   // column of the M = 64 accumulator
-constexpr uint32_t kWgBias = 96;    // column of the bias accumulator
-constexpr uint32_t kOnesBytes = 2048;
 constexpr uint32_t kWgBLine = 3 * 2 * 512;  // per output line: (k, plane) blocks of 32 rows
 
 struct WgradArgs {
@@ -346,7 +346,7 @@ struct WgShape {
     static constexpr uint32_t kXBytes = kXL * kXLine;
     static constexpr uint32_t kBBytes = kWgLB * kWgBLine;
     static constexpr uint32_t kStage = kXBytes + kBBytes;
-    static constexpr uint32_t kSmem = kOnesBytes + kWgStages * kStage;
+    static constexpr uint32_t kSmem = kWgStages * kStage;
 };
 
 __device__ __forceinline__ void wg_block(uint32_t b, const Lp &g, uint32_t &s, uint32_t &x,
@@ -376,8 +376,14 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint32_t bar, uint32_t parity, u
 //     (cores 16..23, of which 16 and 17 are used); one plane: 9 useful cores, one M = 128;
 //   B (MN-major, N = 48): the gradient line at three z shifts, staged as blocks
 //     (k, plane) of 32 rows starting at z' = k (k = 1 - dz) -- N-core (k, plane) at +512 B;
-// so D (48 columns: dz, co) accumulates two (one) MMAs per K step; the bias gradient is an
-// all-ones A against the k = 1 blocks.
+// so D (48 columns: dz, co) accumulates two (one) MMAs per K step.  The bias gradient
+// (the sum of the gradient over voxels) is summed from the staged k = 1 blocks by the
+// epilogue warps, which have nothing else to do until the last MMA: thread t adds
+// channel t % 16 of 16 fixed voxels of every block, and a stage is refilled only after
+// both the MMAs and these four warps have released it.
+// (Measured and dropped: staging only the k = 1 blocks and building the shifted ones in
+// these warps -- 24% fewer TMA bytes -- put the copies on the critical path: 27.1 against
+// 23.8 us for the 16-channel layer.)
 template <int NPLX>
 __global__ void __launch_bounds__(kWgThreads)
     wgrad_tc_kernel(const __grid_constant__ CUtensorMap xmap,
@@ -386,13 +392,10 @@ __global__ void __launch_bounds__(kWgThreads)
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[kWgStages], empty[kWgStages], done;
     __shared__ uint32_t taddr_s;
+    __shared__ float bias_part[8][16];
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    uint8_t *ones = smem;
-    uint8_t *stage_s = smem + kOnesBytes;
+    uint8_t *stage_s = smem;
 
-    for (uint32_t i = tid; i < kOnesBytes / 4; i += kWgThreads)
-        reinterpret_cast<uint32_t *>(ones)[i] = 0x3F803F80u;  // BF16 1.0 pairs
-    fence_async_smem();
     if (warp == 0) {
         tmem_alloc(smem_addr(&taddr_s), kWgCols);
         tmem_relinquish();
@@ -400,7 +403,7 @@ __global__ void __launch_bounds__(kWgThreads)
     if (tid == kWgMma) {
         for (uint32_t i = 0; i < kWgStages; i++) {
             mbar_init(smem_addr(&full[i]), 1);
-            mbar_init(smem_addr(&empty[i]), 1);
+            mbar_init(smem_addr(&empty[i]), 1 + 4);  // the MMA commit + the 4 epilogue warps
         }
         mbar_init(smem_addr(&done), 1);
         mbar_fence_init();
@@ -410,27 +413,11 @@ __global__ void __launch_bounds__(kWgThreads)
     tc_fence_after();
     const uint32_t taddr = taddr_s;
     const bool any = blockIdx.x < a.nblocks;
+    const uint32_t npd = a.dy.npl;
 
-    auto copy = [&](uint32_t st, uint32_t b) {
-        uint32_t s, x, y0;
-        wg_block(b, a.dy, s, x, y0);
-        const uint32_t bar = smem_addr(&full[st]);
-        mbar_expect_tx(bar, S::kXBytes + kWgLB * 3 * a.dy.npl * 512);
-        const uint32_t dst = smem_addr(stage_s + st * S::kStage);
-        const int32_t xg = (int32_t)(s * (a.dy.n0 + 2) + x);
-        tma_load_4d(dst, &xmap, 0, 0, xg, (int32_t)y0, bar);
-        if (a.dy_one_box)  // [line][k][plane][32 rows] in one box (k = a 16-byte shift)
-            tma_load_5d(dst + S::kXBytes, &dymap, 0, 0, 0, (int32_t)(y0 + 1), xg + 1, bar);
-        else
-            for (uint32_t j = 0; j < kWgLB; j++)
-                for (uint32_t k = 0; k < 3; k++)
-                    tma_load_4d(dst + S::kXBytes + j * kWgBLine + k * 1024, &dymap,
-                                (int32_t)(k * 8), 0, (int32_t)(y0 + 1 + j), xg + 1, bar);
-        mbar_arrive(bar);
-    };
     if (tid == kWgTma) {
         // ---- TMA producer: the stage of local block i is i % kWgStages, refilled as soon
-        // as the MMAs of block i - kWgStages have completed
+        // as block i - kWgStages has been released
         uint32_t it = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kWgStages;
@@ -439,14 +426,26 @@ __global__ void __launch_bounds__(kWgThreads)
                 fail(64);
                 break;
             }
-            copy(st, b);
+            uint32_t s, x, y0;
+            wg_block(b, a.dy, s, x, y0);
+            const uint32_t bar = smem_addr(&full[st]);
+            mbar_expect_tx(bar, S::kXBytes + kWgLB * 3 * npd * 512);
+            const uint32_t dst = smem_addr(stage_s + st * S::kStage);
+            const int32_t xg = (int32_t)(s * (a.dy.n0 + 2) + x);
+            tma_load_4d(dst, &xmap, 0, 0, xg, (int32_t)y0, bar);
+            if (a.dy_one_box)  // [line][k][plane][32 rows] in one box (k = a 16-byte shift)
+                tma_load_5d(dst + S::kXBytes, &dymap, 0, 0, 0, (int32_t)(y0 + 1), xg + 1, bar);
+            else
+                for (uint32_t j = 0; j < kWgLB; j++)
+                    for (uint32_t k = 0; k < 3; k++)
+                        tma_load_4d(dst + S::kXBytes + j * kWgBLine + k * 1024, &dymap,
+                                    (int32_t)(k * 8), 0, (int32_t)(y0 + 1 + j), xg + 1, bar);
+            mbar_arrive(bar);
         }
     } else if (tid == kWgMma) {
         // ---- MMA issue
         const uint32_t idesc128 = umma_idesc_bf16(128, 48, true, true);
         const uint32_t idesc64 = umma_idesc_bf16(64, 48, true, true);
-        const uint32_t idesc16 = umma_idesc_bf16(64, 16, true, true);
-        const uint64_t ones_d = umma_smem_desc(smem_addr(ones), 128, 256);
         uint32_t it = 0, acc = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kWgStages;
@@ -467,7 +466,6 @@ __global__ void __launch_bounds__(kWgThreads)
                     const uint64_t ad = ad0 + ((j * S::kXLine + ks * 256) >> 4);
                     umma_bf16(taddr, ad, bd, idesc128, acc);
                     if (NPLX == 2) umma_bf16(taddr + kWgAcc64, ad + ((16 * 512) >> 4), bd, idesc64, acc);
-                    umma_bf16(taddr + kWgBias, ones_d, bd + (1024 >> 4), idesc16, acc);
                     acc = 1;
                 }
             }
@@ -475,50 +473,76 @@ __global__ void __launch_bounds__(kWgThreads)
         }
         umma_commit(smem_addr(&done));
     } else if (tid < 128) {
+        // ---- bias gradient from the staged gradient lines, then the accumulators
+        const uint32_t c = tid % 16, grp = tid / 16;  // channel, voxel group (8 x 16 voxels)
+        const bool chan = c < npd * 8 && c < a.cout;
+        float bsum = 0.0f;
+        bool ok = true;
+        uint32_t it = 0;
+        for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
+            const uint32_t st = it % kWgStages;
+            if (!mbar_wait(smem_addr(&full[st]), (it / kWgStages) & 1, kSpin)) {
+                fail(256);
+                ok = false;
+                break;
+            }
+            const unsigned char *bb = stage_s + st * S::kStage + S::kXBytes;
+            if (chan) {
+                // voxels 16 grp .. 16 grp + 15 of the block's 4 x 32: line j, z
+                const unsigned char *blk = bb + 1024 + (c / 8) * 512 + (c % 8) * 2;
+#pragma unroll
+                for (uint32_t v = 0; v < 16; v++) {
+                    const uint32_t vox = grp * 16 + v, j = vox / 32, z = vox % 32;
+                    const uint16_t h =
+                        *reinterpret_cast<const uint16_t *>(blk + j * kWgBLine + z * 16);
+                    bsum += __uint_as_float((uint32_t)h << 16);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_addr(&empty[st]));
+        }
+        bias_part[grp][c] = bsum;
         float *P = a.partial + (uint64_t)blockIdx.x * a.kp * 16;
-        const bool ok = mbar_wait_sleep(smem_addr(&done), 0, kSpin);
+        ok = mbar_wait_sleep(smem_addr(&done), 0, kSpin) && ok;
         if (!ok) fail(128);
         tc_fence_after();
+        asm volatile("bar.sync 1, 128;" ::: "memory");
         if (!any || !ok) {
             for (uint32_t i = tid; i < a.kp * 16; i += 128) P[i] = 0.0f;
         } else {
-            // chunk c: 0..2 = M = 128 accumulator (k = c), 3..5 = M = 64 (k = c - 3), 6 = bias
-            const uint32_t chunks = NPLX == 2 ? 7 : 4;
-            for (uint32_t c = 0; c < chunks; c++) {
-                const bool bias = c == chunks - 1;
-                const bool m64 = !bias && c >= 3;
+            if (tid < 16) {
+                float bs = 0.0f;
+                for (uint32_t g = 0; g < 8; g++) bs += bias_part[g][tid];
+                P[27 * a.cin * 16 + tid] = tid < npd * 8 ? bs : 0.0f;
+            }
+            // chunk c: 0..2 = M = 128 accumulator (k = c), 3..5 = M = 64 (k = c - 3)
+            const uint32_t chunks = NPLX == 2 ? 6 : 3;
+            for (uint32_t ck = 0; ck < chunks; ck++) {
+                const bool m64 = ck >= 3;
                 float v[16];
                 __syncwarp();
-                tmem_ld16(taddr + ((warp * 32u) << 16) +
-                              (bias ? kWgBias : m64 ? kWgAcc64 + (c - 3) * 16 : c * 16), v);
+                tmem_ld16(taddr + ((warp * 32u) << 16) + (m64 ? kWgAcc64 + (ck - 3) * 16 : ck * 16), v);
                 tmem_ld_wait();
-                uint32_t row = 0;
+                // accumulator row -> M-core i and channel within the core
+                uint32_t i, c8;
                 bool valid;
-                if (bias) {
-                    valid = warp == 0 && lane == 0;
-                    row = 27 * a.cin;
+                if (m64) {
+                    valid = lane < 16;
+                    i = 16 + (warp * 16 + lane) / 8;
+                    c8 = lane % 8;
                 } else {
-                    // accumulator row -> M-core i and channel within the core
-                    uint32_t i, c8;
-                    if (m64) {
-                        valid = lane < 16;
-                        i = 16 + (warp * 16 + lane) / 8;
-                        c8 = lane % 8;
-                    } else {
-                        valid = true;
-                        i = (warp * 32 + lane) / 8;
-                        c8 = lane % 8;
-                    }
-                    const uint32_t dyi = i / (3 * NPLX), dx = (i / NPLX) % 3, h = i % NPLX;
-                    const uint32_t ci = h * 8 + c8;
-                    const uint32_t dzi = 2 - (m64 ? c - 3 : c);  // chunk k holds dz = 1 - k
-                    valid = valid && dyi < 3 && ci < a.cin;
-                    row = (dx * 9 + dyi * 3 + dzi) * a.cin + ci;
+                    valid = true;
+                    i = (warp * 32 + lane) / 8;
+                    c8 = lane % 8;
                 }
+                const uint32_t dyi = i / (3 * NPLX), dx = (i / NPLX) % 3, h = i % NPLX;
+                const uint32_t ci = h * 8 + c8;
+                const uint32_t dzi = 2 - (m64 ? ck - 3 : ck);  // chunk k holds dz = 1 - k
+                valid = valid && dyi < 3 && ci < a.cin;
                 if (valid) {
-                    float *p = P + (uint64_t)row * 16;
+                    float *p = P + (uint64_t)((dx * 9 + dyi * 3 + dzi) * a.cin + ci) * 16;
 #pragma unroll
-                    for (int co = 0; co < 16; co++) p[co] = co < (int)(a.dy.npl * 8) ? v[co] : 0.0f;
+                    for (int co = 0; co < 16; co++) p[co] = co < (int)(npd * 8) ? v[co] : 0.0f;
                 }
             }
         }
