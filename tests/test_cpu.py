@@ -41,6 +41,26 @@ def test_library_exports_reference_cpp_entry_points():
         assert fn in out, fn
 
 
+def test_cnn_line_planes_sizes_and_shape_checks():
+    """Host arithmetic of the tensor-core CNN entry points (no GPU needed): line-planes
+    tensor bytes = (batch (n0+2)(n1+2) + 16 tail lines) x planes x (32 + 2 zpad) rows x
+    16 B; weight images 9 (two-plane input) or 5 (one plane, taps paired) groups of
+    1536 B; volumes that are not 32-voxel z-lines or whose n1 is not a multiple of 8 are
+    refused (0 bytes)."""
+    assert capi.cnn_lp_bytes(16, 0, (32, 32, 32), 16) == (16 * 34 * 34 + 16) * 2 * 32 * 16
+    assert capi.cnn_lp_bytes(1, 1, (32, 32, 32), 16) == (16 * 34 * 34 + 16) * 1 * 34 * 16
+    assert capi.cnn_lp_bytes(2, 0, (3, 8, 32), 2) == (2 * 5 * 10 + 16) * 1 * 32 * 16
+    assert capi.cnn_lp_bytes(16, 0, (32, 32, 16), 1) == 0  # z-lines must be 32 voxels
+    assert capi.cnn_lp_bytes(16, 0, (32, 12, 32), 1) == 0  # n1 % 8 != 0
+    assert capi.cnn_lp_bytes(17, 0, (32, 32, 32), 1) == 0  # at most 16 channels
+    assert capi.cnn_lp_bytes(16, 2, (32, 32, 32), 1) == 0  # zpad 0 or 1
+    assert capi.cnn_tc_weight_bytes(16) == 9 * 1536 and capi.cnn_tc_weight_bytes(9) == 9 * 1536
+    assert capi.cnn_tc_weight_bytes(2) == 5 * 1536 and capi.cnn_tc_weight_bytes(1) == 5 * 1536
+    assert capi.cnn_tc_weight_bytes(0) == 0 and capi.cnn_tc_weight_bytes(17) == 0
+    with pytest.raises(capi.BackprojectorError):  # null tensors: refused before any launch
+        capi.cnn_tc_conv3d(None, 16, 0, (32, 32, 32), 1, None, None, 16, True, d_Y=None)
+
+
 def test_abi_version_and_status_strings():
     L = capi.lib()
     assert L.bpgb_abi_version() == capi.ABI_VERSION == 2
