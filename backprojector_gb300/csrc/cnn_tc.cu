@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kConvThreads)
     } else if (tid == kConvMma) {
         // ---- MMA issue
         const uint32_t idesc = umma_idesc_bf16(128, kConvN, false, false);
-        const uint32_t wbase = smem_addr(w_s);
+        const uint64_t b_base = umma_smem_desc(smem_addr(w_s), kConvN * 16, 128);
         uint32_t it = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kConvStages, ab = it % kConvAccs;
@@ -214,23 +214,25 @@ __global__ void __launch_bounds__(kConvThreads)
                 break;
             }
             tc_fence_after();
-            const uint32_t base = smem_addr(stage_s + st * S::kStage);
             const uint32_t d = taddr + ab * kConvAcc;
+            // descriptors: the stage's base descriptor plus compile-time start and LBO
+            // offsets (the fields cannot carry: addresses stay below 256 KB)
+            const uint64_t a_base = umma_smem_desc(smem_addr(stage_s + st * S::kStage), 0, 128);
 #pragma unroll
             for (uint32_t g = 0; g < S::kGroups; g++) {
-                uint32_t a0, lbo;
+                uint32_t off, lbo;
                 if (NPL == 2) {
-                    a0 = base + (g / 3) * 2 * kConvBox + (g % 3) * 512;
+                    off = (g / 3) * 2 * kConvBox + (g % 3) * 512;
                     lbo = kConvBox;  // plane 1 of the same lines
                 } else {
                     const uint32_t ta = 2 * g, tb = 2 * g + 1;
-                    a0 = base + (ta / 3) * kConvBox + (ta % 3) * 512;
+                    off = (ta / 3) * kConvBox + (ta % 3) * 512;
                     // second K group: the next tap (the tenth is a zero-weight slot that
                     // reads the rows one voxel further on)
-                    lbo = tb < 9 ? base + (tb / 3) * kConvBox + (tb % 3) * 512 - a0 : 16u;
+                    lbo = tb < 9 ? (tb / 3) * kConvBox + (tb % 3) * 512 - off : 16u;
                 }
-                umma_bf16(d, umma_smem_desc(a0, lbo, 128),
-                          umma_smem_desc(wbase + g * kConvGroup, kConvN * 16, 128), idesc, g > 0);
+                umma_bf16(d, a_base + (off >> 4) + ((uint64_t)(lbo >> 4) << 16),
+                          b_base + ((g * kConvGroup) >> 4), idesc, g > 0);
             }
             umma_commit(smem_addr(&empty[st]));
             umma_commit(smem_addr(&acc_full[ab]));
