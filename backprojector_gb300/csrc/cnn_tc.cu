@@ -91,9 +91,9 @@ constexpr uint32_t kConvLB = 4;                       // output lines per block 
 constexpr uint32_t kConvLines = kConvLB + 3;          // y' lines staged per (x', plane), 1 spare
 constexpr uint32_t kConvBox = kConvLines * 32 * 16;   // bytes of one staged (x', plane) box
 constexpr uint32_t kConvStages = 4;
-constexpr uint32_t kConvThreads = 320;                // 8 epilogue warps, MMA warp, TMA warp
-constexpr uint32_t kConvMma = 256;                    // the MMA-issuing thread
-constexpr uint32_t kConvTma = 288;                    // the TMA-issuing thread
+constexpr uint32_t kConvThreads = 352;  // 8 epilogue warps, 2 MMA warps, the TMA warp
+constexpr uint32_t kConvMma = 256;      // MMA-issuing threads: 256 (even blocks), 288 (odd)
+constexpr uint32_t kConvTma = 320;      // the TMA-issuing thread
 constexpr uint32_t kConvN = 48;                       // dz x 16 output channels
 constexpr uint32_t kConvAccs = 4;                     // accumulators in flight
 constexpr uint32_t kConvAcc = 64;                     // columns per accumulator
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kConvThreads)
     using S = ConvShape<NPL>;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t full[kConvStages], empty[kConvStages], acc_full[kConvAccs],
-        acc_empty[kConvAccs], drain;
+        acc_empty[kConvAccs], drain[2], wbar;
     __shared__ uint32_t taddr_s;
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t *w_s = smem;
@@ -164,7 +164,9 @@ __global__ void __launch_bounds__(kConvThreads)
             mbar_init(smem_addr(&acc_full[i]), 1);
             mbar_init(smem_addr(&acc_empty[i]), 128);
         }
-        mbar_init(smem_addr(&drain), 1);
+        mbar_init(smem_addr(&drain[0]), 1);
+        mbar_init(smem_addr(&drain[1]), 1);
+        mbar_init(smem_addr(&wbar), 1);
         mbar_fence_init();
     }
     tc_fence_before();
@@ -172,12 +174,11 @@ __global__ void __launch_bounds__(kConvThreads)
     tc_fence_after();
     const uint32_t taddr = taddr_s;
 
-    auto copy = [&](uint32_t st, uint32_t b, bool weights) {
+    auto copy = [&](uint32_t st, uint32_t b) {
         uint32_t s, x, y0;
         conv_block(b, a.in, s, x, y0);
         const uint32_t bar = smem_addr(&full[st]);
-        mbar_expect_tx(bar, S::kStage + (weights ? S::kWBytes : 0u));
-        if (weights) bulk_g2s(smem_addr(w_s), a.W, S::kWBytes, bar);
+        mbar_expect_tx(bar, S::kStage);
         const uint32_t dst = smem_addr(stage_s + st * S::kStage);
         const int32_t xg = (int32_t)(s * (a.in.n0 + 2) + x);
         // one box: 3 x' x the planes x 7 lines x 32 voxels, landing [dx][plane][line][z]
@@ -185,8 +186,11 @@ __global__ void __launch_bounds__(kConvThreads)
         mbar_arrive(bar);
     };
     if (tid == kConvTma) {
-        // ---- TMA producer: the stage of local block i is i % kConvStages, refilled as
-        // soon as the MMAs of block i - kConvStages have completed
+        // ---- TMA producer: the weights once, then the stage of local block i is
+        // i % kConvStages, refilled as soon as the MMAs of block i - kConvStages completed
+        mbar_expect_tx(smem_addr(&wbar), S::kWBytes);
+        bulk_g2s(smem_addr(w_s), a.W, S::kWBytes, smem_addr(&wbar));
+        mbar_arrive(smem_addr(&wbar));
         uint32_t it = 0;
         for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
             const uint32_t st = it % kConvStages;
@@ -195,14 +199,18 @@ __global__ void __launch_bounds__(kConvThreads)
                 fail(4);
                 break;
             }
-            copy(st, b, it == 0);
+            copy(st, b);
         }
-    } else if (tid == kConvMma) {
-        // ---- MMA issue
+    } else if (tid == kConvMma || tid == kConvMma + 32) {
+        // ---- MMA issue: two threads take alternate blocks (their stages, accumulators
+        // and epilogue groups alternate with them), each committing its own MMAs
+        const uint32_t m = (tid - kConvMma) / 32;
         const uint32_t idesc = umma_idesc_bf16(128, kConvN, false, false);
         const uint64_t b_base = umma_smem_desc(smem_addr(w_s), kConvN * 16, 128);
-        uint32_t it = 0;
-        for (uint32_t b = blockIdx.x; b < a.nblocks; b += gridDim.x, it++) {
+        if (!mbar_wait(smem_addr(&wbar), 0, kSpin)) fail(1);
+        uint32_t it = m;
+        for (uint64_t b = blockIdx.x + (uint64_t)m * gridDim.x; b < a.nblocks;
+             b += 2ull * gridDim.x, it += 2) {
             const uint32_t st = it % kConvStages, ab = it % kConvAccs;
             if (!mbar_wait(smem_addr(&full[st]), (it / kConvStages) & 1, kSpin)) {
                 fail(1);
@@ -237,8 +245,8 @@ __global__ void __launch_bounds__(kConvThreads)
             umma_commit(smem_addr(&empty[st]));
             umma_commit(smem_addr(&acc_full[ab]));
         }
-        umma_commit(smem_addr(&drain));
-        if (!mbar_wait(smem_addr(&drain), 0, kSpin)) fail(8);
+        umma_commit(smem_addr(&drain[m]));
+        if (!mbar_wait(smem_addr(&drain[m]), 0, kSpin)) fail(8);
     } else if (warp < 8) {
         // ---- epilogue: two groups of 4 warps take alternate blocks; in a group, warp q
         // reads tensor-memory lanes 32 q.. (line q of the block), lane = z: one voxel each
