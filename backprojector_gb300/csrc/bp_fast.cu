@@ -10,6 +10,10 @@
 //   * A CTA owns one voxel tile and, when `splits` > 1, a contiguous range of
 //     (laser, SPAD-chunk) items.  Each consumer thread holds K voxels on a line along
 //     one axis (`kax`); a warp's lanes cover the other axes at each step of that line.
+//     The grouped form (preset 13, block-sparse passes) gives a CTA four 8^3 tiles, each
+//     with its own two consumer warps, sharing the producer and the stage ring: a stage
+//     holds `chunk` rows of every tile, so an SM runs as many consumer warps as with the
+//     wide tiles while the tiles stay the size of the occupancy CNN's blocks.
 //   * Warp 0 is the producer.  For every item it computes, per SPAD row of the chunk,
 //     the range of bins the tile can reach (exact distance bounds from the SPAD and
 //     the laser point to the tile's box), aligns it for TMA, writes a 32-byte row record
@@ -27,7 +31,9 @@
 //     That is 6 FP32x2 + 2 MUFU + 2 address + 2 gathers = 12 issue slots per two updates;
 //     FP16/BF16 rows accumulate with sm_100's one-op mixed-precision add.
 //   * Stages are handed over with mbarriers (full: TMA bytes + producer arrive; empty:
-//     one arrive per consumer warp).  Every wait is bounded; a wait that gives up sets
+//     one arrive per consumer warp; the producer sleeps briefly between its polls, so
+//     that they take no issue slots from the consumers).  Every wait is bounded; a wait
+//     that gives up sets
 //     an error counter the host reads (bpgb_plan_check) and the CTA drains its own
 //     in-flight copies before returning.
 //
@@ -58,6 +64,8 @@ constexpr int kBatchRows = 4;  // and the batch kernel
 constexpr int kC32Rows = 4;    // complex rows (FP16 pairs / complex64), whose accumulators
 constexpr int kC64Rows = 1;    // already double the registers
 constexpr uint32_t kMaxChunk = 64;                         // rows per stage (two per lane)
+constexpr uint32_t kMaxGroupEntries = 128;  // grouped stages: (tile, row) entries, four per lane
+constexpr uint32_t kMaxGroups = 4;          // tiles per CTA
 constexpr uint32_t kFactS = 4;  // SPADs per block of the factored lasers x SPADs form
 constexpr uint32_t kRecordBytes = 32;                      // two float4 per row
 constexpr uint32_t kPlanDiagWords = 8;  // a plan's device counters (see fast_plan_build)
@@ -98,10 +106,13 @@ struct FastArgs {
     uint32_t T;
     float out_scale;
     uint64_t nvox;
-    // tile-list launches (block-sparse passes): CTA i runs tile tile_list[i] while
-    // i < *tile_count; null = every tile of the volume
+    // tile-list launches (block-sparse passes): CTA i runs the tiles in list slots
+    // groups x (i / splits) + g (g < groups) below min(*tile_count, max_tiles); null =
+    // every tile of the volume
     const uint32_t *tile_list;
     const uint32_t *tile_count;
+    uint32_t max_tiles;
+    uint32_t groups;  // tiles per CTA, each with its own wx x wy x wz consumer warps
     // tile-list launches with pair splits: partial sums are stored per list slot and
     // split at tile-local voxel offsets (slot-major, then split, then voxel)
     uint32_t tile_local;
@@ -400,22 +411,62 @@ struct PipeShared {
     int *abort_flag;
 };
 
-// One work unit -- a voxel tile and a range of (laser, SPAD-chunk) items -- through the
-// producer / consumer pipeline.  `step` is the CTA's running pipeline step (stage =
-// step % stages, phase = step / stages); consecutive units of a persistent CTA continue
-// it, so the stage ring and its barriers carry over.  Rows of H are read at
-// row_base + l * S + s (the capture's first row in a packed buffer).  Returns false when
-// a bounded wait gave up (the CTA must stop).
-template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int ROWS>
+// Tile and output base of tile g of a CTA's group: tile t0 + g of the volume, or in a
+// tile-list launch the tile in list slot t0 + g (with pair splits, partial sums at the
+// slot's own tile-local block); false when there is none.
+template <typename PairT>
+__device__ __forceinline__ bool group_tile(const FastArgs &a, void *out, uint32_t t0, uint32_t g,
+                                           uint32_t &tile, void *&dst) {
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    dst = out;
+    tile = t0 + g;
+    if (!a.tile_list) return tile < ntiles;
+    const uint32_t slot = t0 + g;
+    if (slot >= a.max_tiles || slot >= *a.tile_count) return false;
+    tile = a.tile_list[slot];
+    if (tile >= ntiles) return false;
+    if (a.tile_local) {
+        constexpr uint32_t kOutEsz = PairT::kCplx ? 8 : 4;
+        const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
+        dst = (unsigned char *)out + (uint64_t)slot * a.splits * tvox * kOutEsz;
+    }
+    return true;
+}
+
+// First tile (full-volume launch) or list slot (tile-list launch) of a grouped CTA's
+// tiles, and its pair split.
+__device__ __forceinline__ uint32_t group_origin(const FastArgs &a, uint32_t &split) {
+    if (a.tile_list) {
+        split = blockIdx.x % a.splits;
+        return blockIdx.x / a.splits * a.groups;
+    }
+    const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    const uint64_t ngroups = (ntiles + a.groups - 1) / a.groups;
+    split = (uint32_t)(blockIdx.x / ngroups);
+    return (uint32_t)(blockIdx.x % ngroups) * a.groups;
+}
+
+// One work unit -- a voxel tile (group_tile(t0, 0)) and a range of (laser, SPAD-chunk)
+// items -- through the producer / consumer pipeline.  GROUPED: a group of a.groups tiles
+// (group_tile(t0, g)), each with its own wx x wy x wz consumer warps; a stage then holds
+// `chunk` rows for every tile of the group, entry e = g x chunk + row (record and
+// window), so one producer and one stage ring serve them all.  `step` is the CTA's
+// running pipeline step (stage = step % stages, phase = step / stages); consecutive units
+// of a persistent CTA continue it, so the stage ring and its barriers carry over.  Rows
+// of H are read at row_base + l * S + s (the capture's first row in a packed buffer).
+// Returns false when a bounded wait gave up (the CTA must stop).
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int ROWS, bool GROUPED>
 __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *tmap,
                                           const float4 *__restrict__ spads,
                                           const float4 *__restrict__ lasers, void *out,
-                                          unsigned long long *diag, uint32_t tile,
+                                          unsigned long long *diag, uint32_t t0,
                                           uint32_t split, uint32_t row_base, uint64_t &step,
                                           const PipeShared &sh) {
     using PairT = Pair<HT>;
     constexpr uint32_t esz = PairT::kEsz;
     constexpr int NP = K / 2;
+    // stage entries per producer lane
+    constexpr uint32_t kLane = GROUPED ? kMaxGroupEntries / 32 : kMaxChunk / 32;
     unsigned char *const smem_raw = sh.smem_raw;
     unsigned char *const stage_base = sh.stage_base;
     const uint32_t pad = sh.pad;
@@ -431,10 +482,32 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
     const uint32_t count = (uint32_t)(i1 - i0);  // items < 2^32 (checked at plan build)
 
     TileGeo g;
-    tile_of_block(a, tile, g);
+    uint32_t tile = t0;  // the tile itself when not GROUPED
+    if constexpr (!GROUPED) tile_of_block(a, tile, g);
 
     if (warp == 0) {
         // ---------------- producer ----------------
+        // GROUPED: entry lane + 32 q of a stage is row (lane + 32 q) % chunk of tile
+        // (lane + 32 q) / chunk of the group, whose geometry (and whether it exists) the
+        // producer keeps in shared memory for the unit
+        uint32_t nvalid = 1;  // tiles of the group that exist
+        const TileGeo *geo = nullptr;
+        const uint32_t *geo_ok = nullptr;
+        uint32_t cshift = 0;
+        if constexpr (GROUPED) {
+            __shared__ TileGeo geo_s[kMaxGroups];
+            __shared__ uint32_t ok_s[kMaxGroups];
+            if (lane < kMaxGroups) {
+                void *unused;
+                ok_s[lane] = lane < a.groups && group_tile<PairT>(a, out, t0, lane, tile, unused);
+                if (ok_s[lane]) tile_of_block(a, tile, geo_s[lane]);
+            }
+            __syncwarp();
+            nvalid = ok_s[0] + ok_s[1] + ok_s[2] + ok_s[3];
+            geo = geo_s;
+            geo_ok = ok_s;
+            cshift = __ffs(a.chunk) - 1;  // chunk = 2^cshift
+        }
         // stage / round of the ring and (laser, chunk) of the item advance by counting: no
         // 64-bit division per stage
         uint32_t stage = (uint32_t)(step0 % a.stages);
@@ -446,8 +519,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             if (round > 0) {
                 // Every lane observes the consumers' release before its TMA overwrites
                 // the stage.
-                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (uint32_t)(round - 1) & 1,
-                                    a.spin_limit);
+                bool ok = mbar_wait_backoff(smem_addr(&empty_bar[stage]),
+                                            (uint32_t)(round - 1) & 1, a.spin_limit);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
@@ -469,34 +542,59 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
             float4 *table = reinterpret_cast<float4 *>(st);
             const uint32_t data = smem_addr(st + a.table_bytes);
             const uint32_t fb = smem_addr(&full_bar[stage]);
-            // rows lane and lane + 32 of the chunk (kMaxChunk = 64)
-            int32_t lo[kMaxChunk / 32] = {};
-#pragma unroll
-            for (uint32_t q = 0; q < kMaxChunk / 32; q++) {
-                const uint32_t r = lane + 32 * q;
-                if (r < nrows) {
-                    const float4 G = spads[s0 + r];
-                    const float4 Lt = lasers[l];
-                    float e[3], ew;
-                    lo[q] = row_record(a, g, G, Lt, e, ew);
-                    const float ek = sel3(e[0], e[1], e[2], a.kax);
-                    table[2 * r] = make_float4(sel3(e[0], e[1], e[2], a.oax0),
-                                               sel3(e[0], e[1], e[2], a.oax1), ew, ew);
-                    table[2 * r + 1] = make_float4(-ek, -ek, ew, ew);
+            if constexpr (GROUPED) {
+                // one entry at a time (four per lane): record, then its window
+                if (lane == 0) mbar_expect_tx(fb, nrows * nvalid * a.nbox * a.BW * esz);
+                __syncwarp();
+#pragma unroll 1
+                for (uint32_t q = 0; q < kLane; q++) {
+                    const uint32_t e = lane + 32 * q, r = e & (a.chunk - 1), gi = e >> cshift;
+                    if (r < nrows && gi < kMaxGroups && geo_ok[gi]) {
+                        const float4 G = spads[s0 + r];
+                        const float4 Lt = lasers[l];
+                        float ev[3], ew;
+                        const int32_t lo = row_record(a, geo[gi], G, Lt, ev, ew);
+                        const float ek = sel3(ev[0], ev[1], ev[2], a.kax);
+                        table[2 * e] = make_float4(sel3(ev[0], ev[1], ev[2], a.oax0),
+                                                   sel3(ev[0], ev[1], ev[2], a.oax1), ew, ew);
+                        table[2 * e + 1] = make_float4(-ek, -ek, ew, ew);
+                        const int32_t row = (int32_t)(row_base + l * a.S + s0 + r);
+                        const uint32_t dst = data + e * a.row_bytes;
+                        for (uint32_t b = 0; b < a.nbox; b++)
+                            tma_load_2d(dst + b * a.BW * esz, tmap, lo + (int32_t)(b * a.BW),
+                                        row, fb);
+                    }
                 }
-            }
-            __syncwarp();
-            if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
-            __syncwarp();
+            } else {
+                // entries lane + 32 q of the stage: row r of the chunk
+                int32_t lo[kLane] = {};
 #pragma unroll
-            for (uint32_t q = 0; q < kMaxChunk / 32; q++) {
-                const uint32_t r = lane + 32 * q;
-                if (r < nrows) {
-                    const int32_t row = (int32_t)(row_base + l * a.S + s0 + r);
-                    const uint32_t dst = data + r * a.row_bytes;
-                    for (uint32_t b = 0; b < a.nbox; b++)
-                        tma_load_2d(dst + b * a.BW * esz, tmap, lo[q] + (int32_t)(b * a.BW), row,
-                                    fb);
+                for (uint32_t q = 0; q < kLane; q++) {
+                    const uint32_t e = lane + 32 * q, r = e;
+                    if (r < nrows) {
+                        const float4 G = spads[s0 + r];
+                        const float4 Lt = lasers[l];
+                        float ev[3], ew;
+                        lo[q] = row_record(a, g, G, Lt, ev, ew);
+                        const float ek = sel3(ev[0], ev[1], ev[2], a.kax);
+                        table[2 * e] = make_float4(sel3(ev[0], ev[1], ev[2], a.oax0),
+                                                   sel3(ev[0], ev[1], ev[2], a.oax1), ew, ew);
+                        table[2 * e + 1] = make_float4(-ek, -ek, ew, ew);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) mbar_expect_tx(fb, nrows * a.nbox * a.BW * esz);
+                __syncwarp();
+#pragma unroll
+                for (uint32_t q = 0; q < kLane; q++) {
+                    const uint32_t e = lane + 32 * q, r = e;
+                    if (r < nrows) {
+                        const int32_t row = (int32_t)(row_base + l * a.S + s0 + r);
+                        const uint32_t dst = data + e * a.row_bytes;
+                        for (uint32_t b = 0; b < a.nbox; b++)
+                            tma_load_2d(dst + b * a.BW * esz, tmap, lo[q] + (int32_t)(b * a.BW),
+                                        row, fb);
+                    }
                 }
             }
             __syncwarp();
@@ -507,7 +605,22 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         return true;
     }
     // ---------------- consumers ----------------
-    const uint32_t cw = warp - 1;
+    // GROUPED: warp cw of tile grp = (warp - 1) / (wx wy wz) of the group, reading that
+    // tile's entries of each stage (records and windows grp x chunk ..)
+    uint32_t cw = warp - 1, grp = 0;
+    bool live = true;
+    unsigned char *tab_base = stage_base;
+    uint32_t data_base = pad;  // offset from smem_raw
+    if constexpr (GROUPED) {
+        const uint32_t twarps = a.warp[0] * a.warp[1] * a.warp[2];
+        grp = cw / twarps;
+        cw -= grp * twarps;
+        void *unused;
+        live = group_tile<PairT>(a, out, t0, grp, tile, unused);
+        tile_of_block(a, live ? tile : 0u, g);
+        tab_base += grp * a.chunk * kRecordBytes;
+        data_base += grp * a.chunk * a.row_bytes;
+    }
     const uint32_t li[3] = {lane % a.lane[0], (lane / a.lane[0]) % a.lane[1],
                             lane / (a.lane[0] * a.lane[1])};
     const uint32_t wi[3] = {cw % a.warp[0], (cw / a.warp[0]) % a.warp[1],
@@ -588,9 +701,9 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         const uint64_t s0 = (uint64_t)c * a.chunk;
         const uint32_t nrows =
             (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
-        const unsigned char *st = stage_base + (size_t)stage * a.stage_bytes;
-        const float4 *table = reinterpret_cast<const float4 *>(st);
-        const uint32_t data = pad + stage * a.stage_bytes + a.table_bytes;  // offset from smem_raw
+        const float4 *table =
+            reinterpret_cast<const float4 *>(tab_base + (size_t)stage * a.stage_bytes);
+        const uint32_t data = data_base + stage * a.stage_bytes + a.table_bytes;
 
         PairT part[NP];
         if (KAHAN) {
@@ -601,8 +714,9 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         // voxel-pair chains to interleave (one row for complex rows, whose accumulators
         // already double the registers).  Measured on the 256^3 capture: 2 rows 86.7 ms,
         // 4 rows 84.5, 8 rows 80.9, 16 rows 80.4 (the batch kernel: 4 rows best).
+        const uint32_t jn = live ? nrows : 0u;  // a tile past the list or volume idles
 #pragma unroll(PairT::kCplx ? (PairT::kEsz == 8 ? kC64Rows : kC32Rows) : ROWS)
-        for (uint32_t j = 0; j < nrows; j++) {
+        for (uint32_t j = 0; j < jn; j++) {
             const float4 r0 = table[2 * j];  // (c_o0, c_o1, ew, ew)
             const float D = row_d(v0, v1, r0.x, r0.y);
             const float2 D2 = make_float2(D, D);
@@ -662,6 +776,12 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
         for (int p = 0; p < NP; p++) acc[p].finish(comp[p]);
     }
     const float scale = a.splits > 1 ? 1.0f : a.out_scale;
+    if constexpr (GROUPED) {  // the tile's output base, re-derived rather than held
+        if (!live) return true;
+        uint32_t sp;
+        const uint32_t tw = a.warp[0] * a.warp[1] * a.warp[2];
+        group_tile<PairT>(a, out, group_origin(a, sp), (threadIdx.x / 32 - 1) / tw, tile, out);
+    }
     const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
     const uint64_t part_off = a.splits > 1 ? (uint64_t)split * (a.tile_local ? tvox : a.nvox) : 0;
 #pragma unroll
@@ -954,18 +1074,25 @@ __device__ __forceinline__ bool plan_block(const FastArgs &a, void *out, uint32_
     split = (uint32_t)(blockIdx.x / ntiles);
     dst = out;
     if (a.tile_list) {
-        const uint32_t slot = blockIdx.x / a.splits;
-        if (slot >= *a.tile_count) return false;
-        tile = a.tile_list[slot];
         split = blockIdx.x % a.splits;
-        if (tile >= ntiles) return false;
-        if (a.tile_local) {
-            constexpr uint32_t kOutEsz = PairT::kCplx ? 8 : 4;
-            const uint64_t tvox = (uint64_t)a.tdim[0] * a.tdim[1] * a.tdim[2];
-            dst = (unsigned char *)out + (uint64_t)slot * a.splits * tvox * kOutEsz;
-        }
+        return group_tile<PairT>(a, out, blockIdx.x / a.splits, 0, tile, dst);
     }
     return true;
+}
+
+// Grouped launches: the CTA's first tile (full-volume launch) or list slot (tile-list
+// launch) and pair split; false when none of its group's tiles exists.
+template <typename PairT>
+__device__ __forceinline__ bool plan_group(const FastArgs &a, void *out, uint32_t &t0,
+                                           uint32_t &split) {
+    t0 = group_origin(a, split);
+    bool any = false;
+    for (uint32_t g = 0; g < a.groups; g++) {
+        uint32_t tile;
+        void *dst;
+        any = any || group_tile<PairT>(a, out, t0, g, tile, dst);
+    }
+    return any;
 }
 
 // Stage ring (128-byte aligned) and its mbarriers; ends with a CTA barrier.
@@ -989,8 +1116,9 @@ __device__ __forceinline__ void pipeline_init(PipeShared &sh, unsigned char *sme
     __syncthreads();
 }
 
-// CTAS: resident CTAs per SM the variant is compiled for (its register budget).
-template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int CTAS>
+// CTAS: resident CTAs per SM the variant is compiled for (its register budget).  GROUPED:
+// several tiles per CTA (fast_unit).
+template <typename HT, int K, bool KAHAN, bool CHECKED, bool PLANAR, int CTAS, bool GROUPED>
 __global__ void __launch_bounds__(288, CTAS)
     bp_fast_kernel(const __grid_constant__ CUtensorMap tmap, const float4 *__restrict__ spads,
                    const float4 *__restrict__ lasers, void *__restrict__ out,
@@ -999,14 +1127,18 @@ __global__ void __launch_bounds__(288, CTAS)
     __shared__ __align__(8) uint64_t full_bar[8];
     __shared__ __align__(8) uint64_t empty_bar[8];
     __shared__ int abort_flag;
-    uint32_t tile, split;
-    void *dst;
-    if (!plan_block<Pair<HT>>(a, out, tile, split, dst)) return;
+    uint32_t t0, split;
+    void *dst = out;
+    if constexpr (GROUPED) {
+        if (!plan_group<Pair<HT>>(a, out, t0, split)) return;
+    } else {
+        if (!plan_block<Pair<HT>>(a, out, t0, split, dst)) return;
+    }
     PipeShared sh;
     pipeline_init(sh, smem_raw, full_bar, empty_bar, &abort_flag, a.stages);
     uint64_t step = 0;
-    fast_unit<HT, K, KAHAN, CHECKED, PLANAR, kPlanRows>(a, &tmap, spads, lasers, dst, diag, tile,
-                                                        split, 0, step, sh);
+    fast_unit<HT, K, KAHAN, CHECKED, PLANAR, kPlanRows, GROUPED>(a, &tmap, spads, lasers, dst,
+                                                                 diag, t0, split, 0, step, sh);
     pipeline_drain(a.stages, step, full_bar, diag, a.spin_limit);
 }
 
@@ -1072,6 +1204,7 @@ __global__ void reduce_tiles_kernel(const float *__restrict__ partial,
         const uint64_t local = r / C;
         const uint32_t c = (uint32_t)(r - local * C);
         const uint32_t tile = list[slot];
+        if (tile >= (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2]) continue;  // skipped entry
         const uint32_t tz = tile % a.tiles[2], tx = (tile / a.tiles[2]) % a.tiles[0],
                        ty = tile / (a.tiles[2] * a.tiles[0]);
         const uint32_t lz = (uint32_t)(local % a.tdim[2]),
@@ -1336,42 +1469,57 @@ const FastConfig kPresets[] = {
     {8, 1, 4, 8, 1, 1, 2, 1, 64, 4},  // 8 x 8 x 8
     {8, 1, 4, 8, 1, 1, 4, 1, 64, 4},  // 8 x 8 x 16
     {8, 1, 4, 8, 2, 1, 2, 1, 64, 4},  // 16 x 8 x 8
+    // 8 x 8 x 8 tiles, four per CTA (2 consumer warps each, one producer and stage ring)
+    {8, 1, 4, 8, 1, 1, 2, 1, 32, 2, 4},
 };
 
-// wide: a preset with 8 consumer warps (three CTAs per SM unless Kahan-compensated)
+// wide: a preset with 8 consumer warps per CTA (three CTAs per SM unless
+// Kahan-compensated); grouped: several tiles per CTA, built for real rows with plain sums
 template <typename HT, int K, bool PLANAR>
-void *kernel_ptr(bool kahan, bool checked, bool wide) {
+void *kernel_ptr(bool kahan, bool checked, bool wide, bool grouped) {
+    if (grouped) {
+        if constexpr (K != 8 || Pair<HT>::kCplx) {
+            return nullptr;
+        } else {
+            if (kahan || !wide) return nullptr;
+            return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 3, true>
+                           : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 3, true>;
+        }
+    }
     if (kahan)
-        return checked ? (void *)bp_fast_kernel<HT, K, true, true, PLANAR, 2>
-                       : (void *)bp_fast_kernel<HT, K, true, false, PLANAR, 2>;
+        return checked ? (void *)bp_fast_kernel<HT, K, true, true, PLANAR, 2, false>
+                       : (void *)bp_fast_kernel<HT, K, true, false, PLANAR, 2, false>;
     if (wide)
-        return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 3>
-                       : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 3>;
-    return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 2>
-                   : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 2>;
+        return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 3, false>
+                       : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 3, false>;
+    return checked ? (void *)bp_fast_kernel<HT, K, false, true, PLANAR, 2, false>
+                   : (void *)bp_fast_kernel<HT, K, false, false, PLANAR, 2, false>;
 }
 
 template <typename HT>
-void *kernel_ptr8(bool kahan, bool checked, bool planar, bool wide) {
-    return planar ? kernel_ptr<HT, 8, true>(kahan, checked, wide)
-                  : kernel_ptr<HT, 8, false>(kahan, checked, wide);
+void *kernel_ptr8(bool kahan, bool checked, bool planar, bool wide, bool grouped) {
+    return planar ? kernel_ptr<HT, 8, true>(kahan, checked, wide, grouped)
+                  : kernel_ptr<HT, 8, false>(kahan, checked, wide, grouped);
 }
 
 // Variants built: K = 8 for every row type, accumulation, check mode and wall shape, in
-// the 72-register (8-warp presets, plain sums) and 96-register builds; K = 16 (one CTA
-// per SM, 16 chains per thread) for FP32 rows with plain sums.
-void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar, bool wide) {
+// the 72-register (8-warp presets, plain sums) and 96-register builds, plus the grouped
+// form (several tiles per CTA) for real rows with plain sums; K = 16 (one CTA per SM, 16
+// chains per thread) for FP32 rows with plain sums.
+void *select_kernel(int dtype, bool kahan, bool checked, uint32_t k, bool planar, bool wide,
+                    bool grouped = false) {
     if (k == 16) {
-        if (dtype != BPGB_DTYPE_F32 || kahan) return nullptr;
-        return checked ? (void *)bp_fast_kernel<float, 16, false, true, false, 1>
-                       : (void *)bp_fast_kernel<float, 16, false, false, false, 1>;
+        if (dtype != BPGB_DTYPE_F32 || kahan || grouped) return nullptr;
+        return checked ? (void *)bp_fast_kernel<float, 16, false, true, false, 1, false>
+                       : (void *)bp_fast_kernel<float, 16, false, false, false, 1, false>;
     }
     switch (dtype) {
-        case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar, wide);
-        case BPGB_DTYPE_BF16: return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar, wide);
-        case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar, wide);
-        case BPGB_DTYPE_C32: return kernel_ptr8<__half2>(kahan, checked, planar, wide);
-        default: return kernel_ptr8<float>(kahan, checked, planar, wide);
+        case BPGB_DTYPE_F16: return kernel_ptr8<__half>(kahan, checked, planar, wide, grouped);
+        case BPGB_DTYPE_BF16:
+            return kernel_ptr8<__nv_bfloat16>(kahan, checked, planar, wide, grouped);
+        case BPGB_DTYPE_C64: return kernel_ptr8<float2>(kahan, checked, planar, wide, grouped);
+        case BPGB_DTYPE_C32: return kernel_ptr8<__half2>(kahan, checked, planar, wide, grouped);
+        default: return kernel_ptr8<float>(kahan, checked, planar, wide, grouped);
     }
 }
 
@@ -1401,11 +1549,13 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     };
     (void)t0;
     a = FastArgs{};
-    const uint32_t cwarps = cfg.wx * cfg.wy * cfg.wz;
+    const uint32_t cwarps = cfg.cta_consumer_warps();
     if ((cfg.k != 8 && cfg.k != 16) || (cfg.k == 16 && (esz != 4 || kahan || cwarps != 8)) ||
         cfg.lx * cfg.ly * cfg.lz != 32 || cfg.kaxis > 2 ||
-        (cwarps != 8 && cwarps != 4 && cwarps != 2))
+        (cwarps != 8 && cwarps != 4 && cwarps != 2) ||
+        (cfg.groups != 1 && cfg.groups != 2 && cfg.groups != 4) || (cfg.groups > 1 && fact))
         return no("tile preset not available for this row type");
+    a.groups = cfg.groups;
     const uint32_t lane[3] = {cfg.lx, cfg.ly, cfg.lz}, warp[3] = {cfg.wx, cfg.wy, cfg.wz};
     for (int k = 0; k < 3; k++) {
         a.n[k] = vol.n[k];
@@ -1453,9 +1603,15 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     if (a.BW > 256) return no("window box too wide");
     a.W = a.BW * a.nbox;
     a.row_bytes = a.W * esz;
-    auto stage_bytes = [&](uint32_t c) { return table_bytes_of(c) + c * a.row_bytes; };
+    // a stage holds `chunk` rows of each of the group's tiles (kMaxChunk entries at most,
+    // kMaxGroupEntries with several tiles per CTA)
+    auto stage_bytes = [&](uint32_t c) {
+        return table_bytes_of(c * a.groups) + c * a.groups * a.row_bytes;
+    };
+    const uint32_t max_entries = a.groups > 1 ? kMaxGroupEntries : kMaxChunk;
     uint32_t chunk = (uint32_t)std::min<uint64_t>(
-        std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, kMaxChunk), fact ? L * kFactS : S);
+        std::min<uint32_t>(chunk_req ? chunk_req : cfg.chunk, max_entries / a.groups),
+        fact ? L * kFactS : S);
     uint32_t stages = std::min<uint32_t>(stages_req ? stages_req : cfg.stages, 8);
     if (stages < 2) stages = 2;
     // Shared memory per CTA so that the variant's resident-CTA target fits one SM (228 KB).
@@ -1483,9 +1639,14 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
         if (chunk < kFactS || S % kFactS) return no("factored form needs 4-SPAD blocks");
         chunk = chunk / kFactS * kFactS;
     }
+    if (a.groups > 1) {  // a power of two: entry -> (tile, row) by shift and mask
+        uint32_t p2 = 1;
+        while (2 * p2 <= chunk) p2 *= 2;
+        chunk = p2;
+    }
     a.chunk = chunk;
     a.stages = stages;
-    a.table_bytes = table_bytes_of(chunk);
+    a.table_bytes = table_bytes_of(chunk * a.groups);
     a.stage_bytes = stage_bytes(chunk);
     a.fact = fact ? 1 : 0;
     // items: (laser, SPAD chunk), or (SPAD block, laser group) in the factored form
@@ -1496,7 +1657,7 @@ int fast_args(FastArgs &a, const FastConfig &cfg, const Volume &vol, const doubl
     return BPGB_OK;
 }
 
-uint32_t fast_threads(const FastConfig &cfg) { return 32 * (1 + cfg.wx * cfg.wy * cfg.wz); }
+uint32_t fast_threads(const FastConfig &cfg) { return 32 * (1 + cfg.cta_consumer_warps()); }
 uint32_t fast_smem(const FastArgs &a) { return a.stages * a.stage_bytes + 128; }
 
 }  // namespace
@@ -1525,13 +1686,14 @@ struct FastPlan {
     uint32_t k = 8;
     bool planar = false;
     bool fact = false;
-    bool wide = true;  // 8 consumer warps per CTA
+    bool wide = true;      // 8 consumer warps per CTA
+    bool grouped = false;  // several tiles per CTA
 };
 
 void *plan_kernel(const FastPlan *fp) {
     return fp->fact ? select_fact_kernel(fp->dtype, fp->checked)
                     : select_kernel(fp->dtype, fp->kahan, fp->checked, fp->k, fp->planar,
-                                    fp->wide);
+                                    fp->wide, fp->grouped);
 }
 
 int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
@@ -1562,7 +1724,8 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
     // Lasers x SPADs captures take the factored form where it is built: K = 8 voxels per
     // thread, 8 consumer warps, real rows with FP32 sums, whole 4-SPAD blocks.
     const bool fact = fz.geom == GEOM_EXHAUSTIVE && !opt.unfactored && cfg.k == 8 &&
-                      cfg.consumer_warps() == 8 && opt.accum != BPGB_ACCUM_KAHAN &&
+                      cfg.groups == 1 && cfg.consumer_warps() == 8 &&
+                      opt.accum != BPGB_ACCUM_KAHAN &&
                       (dt == BPGB_DTYPE_F32 || dt == BPGB_DTYPE_F16 || dt == BPGB_DTYPE_BF16) &&
                       fz.S % kFactS == 0;
     FastArgs a;
@@ -1585,7 +1748,8 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
     fp->smem = fast_smem(a);
 
     fp->k = cfg.k;
-    fp->wide = cfg.consumer_warps() == 8;
+    fp->wide = cfg.cta_consumer_warps() == 8;
+    fp->grouped = cfg.groups > 1;
     // Device tables: SPAD entries (frame position relative to zero, row constant) and
     // laser entries (frame position, lw/dT - t0/dT), built in FP64 on the GPU from the
     // plan's device pair list (tables_fp64_kernel), which also tests the planar wall:
@@ -1639,19 +1803,20 @@ int fast_plan_build(FastPlan **out, const bpgb_pair *d_pairs, uint64_t P,
     }
 
     const uint64_t ntiles = (uint64_t)a.tiles[0] * a.tiles[1] * a.tiles[2];
+    const uint64_t ngroups = (ntiles + a.groups - 1) / a.groups;  // CTAs per pair split
     const uint64_t items = fast_items(a);
     uint64_t splits = opt.pair_splits > 0 ? (uint64_t)opt.pair_splits : 1;
     if (opt.pair_splits <= 0) {
         const uint64_t want = 2ull * sm_count * occ;  // two waves of resident CTAs
-        if (ntiles < want) splits = (want + ntiles - 1) / ntiles;
+        if (ngroups < want) splits = (want + ngroups - 1) / ngroups;
     }
     splits = std::max<uint64_t>(1, std::min<uint64_t>(splits, items));
-    if (ntiles * splits >= (1ull << 31)) {
+    if (ngroups * splits >= (1ull << 31)) {
         fast_plan_free(fp);
         return no("grid too large");
     }
     a.splits = (uint32_t)splits;
-    fp->grid = (uint32_t)(ntiles * splits);
+    fp->grid = (uint32_t)(ngroups * splits);
     fp->a = a;
 
     // partial sums: [split][voxel] for full launches, [slot][split][tile voxel] for
@@ -1717,7 +1882,8 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     const uint64_t ntiles = (uint64_t)a0.tiles[0] * a0.tiles[1] * a0.tiles[2];
     if (!d_list || !d_count) return set_error(BPGB_ERR_INVALID_ARGUMENT, "null tile list");
     if (max_tiles == 0) return BPGB_OK;
-    if ((uint64_t)max_tiles * a0.splits >= (1ull << 31))
+    const uint64_t slot_groups = ((uint64_t)max_tiles + a0.groups - 1) / a0.groups;
+    if (slot_groups * a0.splits >= (1ull << 31))
         return set_error(BPGB_ERR_UNSUPPORTED, "tile list x pair splits too large for one grid");
     if (max_tiles > ntiles)
         return set_error(BPGB_ERR_INVALID_ARGUMENT, "max_tiles exceeds the plan's tile count");
@@ -1728,6 +1894,7 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     FastArgs a = a0;
     a.tile_list = d_list;
     a.tile_count = d_count;
+    a.max_tiles = max_tiles;
     a.tile_local = a.splits > 1 ? 1 : 0;
     const float4 *spads = fp->d_tables;
     const float4 *lasers = fp->d_tables + a.S;
@@ -1735,8 +1902,8 @@ int fast_plan_execute_tiles(FastPlan *fp, const void *d_H, void *d_out, const ui
     void *kern = plan_kernel(fp);
     void *args[] = {(void *)&map, (void *)&spads, (void *)&lasers, (void *)&target,
                     (void *)&fp->d_diag, (void *)&a};
-    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3(max_tiles * a.splits), dim3(fp->threads), args,
-                                   fp->smem, stream));
+    BPGB_CUDA_TRY(cudaLaunchKernel(kern, dim3((uint32_t)(slot_groups * a.splits)),
+                                   dim3(fp->threads), args, fp->smem, stream));
     count_launches(1);
     if (a.splits > 1) {
         const bool cplx = fp->dtype == BPGB_DTYPE_C64 || fp->dtype == BPGB_DTYPE_C32;
@@ -2028,7 +2195,7 @@ __global__ void __launch_bounds__(288, FACT ? kFactCtas : 3)
             ok = fact_unit<HT, CHECKED>(cap_s.a, &tmap, tab, tab + cap_s.a.S, dst, diag, u.tile,
                                         u.split, (uint32_t)cap_s.row_base, step, sh);
         else
-            ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows>(
+            ok = fast_unit<HT, 8, false, CHECKED, PLANAR, kBatchRows, false>(
                 cap_s.a, &tmap, tab, tab + cap_s.a.S, dst, diag, u.tile, u.split,
                 (uint32_t)cap_s.row_base, step, sh);
         if (!ok) *(volatile int *)&abort_flag = 1;
@@ -2200,7 +2367,7 @@ int bpgb_batch_create(bpgb_batch *out, const bpgb_capture_geometry *caps, uint32
     const uint32_t esz = dtype_bytes(o.h_dtype);
     const uint32_t bw = 128 / esz;
     FastConfig cfg = fast_preset(o.tile, o.h_dtype);
-    if (cfg.k != 8 || cfg.consumer_warps() != 8) cfg = fast_preset(0, o.h_dtype);
+    if (cfg.k != 8 || cfg.consumer_warps() != 8 || cfg.groups != 1) cfg = fast_preset(0, o.h_dtype);
     auto *b = new bpgb_batch_s();
     b->n = n;
     b->dtype = o.h_dtype;

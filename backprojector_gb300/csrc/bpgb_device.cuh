@@ -55,6 +55,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
     return false;
 }
 
+// The same wait with a short sleep between polls, for a warp whose wait is long against
+// its own work (a producer waiting for consumers to release a stage): its polls would
+// otherwise take issue slots from the warps it waits for.
+__device__ __forceinline__ bool mbar_wait_backoff(uint32_t bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t i = 0; i < limit; i++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        __nanosleep(128);
+    }
+    return false;
+}
+
 // 2-D tiled TMA load of a {box, 1} tile at (x, y) into shared memory, completing on bar.
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int32_t x,
                                             int32_t y, uint32_t bar) {

@@ -88,14 +88,16 @@ struct FastConfig {
     // lane layout inside a warp (product 32), voxels per thread (k) on a line along
     // axis `kaxis`, consumer warp layout
     uint32_t lx, ly, lz, k, wx, wy, wz, kaxis;
-    uint32_t chunk;   // SPAD rows per pipeline stage (<= 32)
+    uint32_t chunk;   // SPAD rows per pipeline stage and tile (<= 64 / groups)
     uint32_t stages;  // pipeline depth
+    uint32_t groups = 1;  // tiles per CTA, each with its own wx x wy x wz consumer warps
     uint32_t tile(int a) const {
         const uint32_t l = a == 0 ? lx : (a == 1 ? ly : lz);
         const uint32_t w = a == 0 ? wx : (a == 1 ? wy : wz);
         return l * w * ((uint32_t)a == kaxis ? k : 1);
     }
-    uint32_t consumer_warps() const { return wx * wy * wz; }
+    uint32_t consumer_warps() const { return wx * wy * wz; }  // per tile
+    uint32_t cta_consumer_warps() const { return wx * wy * wz * groups; }
 };
 
 // Tile presets; index -1 selects the tuned default for the geometry.

@@ -146,7 +146,9 @@ int bpgb_octree_create(bpgb_octree *out, const bpgb_pair *pairs, uint64_t num_pa
     int st = bpgb_plan_create(&oc->coarse_plan, pairs, num_pairs, T, oc->coarse, volume_zero_pos,
                               inc_c, t0, deltaT, &po);
     if (st) return fail(st);
-    po.tile = o.tile >= 0 ? o.tile : 10;  // 8^3 tiles = the CNN's blocks
+    // 8^3 tiles = the CNN's blocks: four per CTA (preset 13) for plain sums, one per CTA
+    // (preset 10) where the grouped form is not built (Kahan-compensated sums)
+    po.tile = o.tile >= 0 ? o.tile : (o.accum == BPGB_ACCUM_KAHAN ? 10 : 13);
     po.pair_splits = (int32_t)oc->pair_splits;
     po.chunk = o.chunk;
     po.stages = o.stages;

@@ -314,7 +314,8 @@ int bpgb_batch_autotune(const bpgb_capture_geometry *captures, uint32_t n, const
     };
     std::vector<int> tiles;
     for (int t = 0; t < fast_preset_count(); t++)
-        if (fast_preset(t, base.h_dtype).k == 8 && fast_preset(t, base.h_dtype).consumer_warps() == 8)
+        if (fast_preset(t, base.h_dtype).k == 8 && fast_preset(t, base.h_dtype).consumer_warps() == 8 &&
+            fast_preset(t, base.h_dtype).groups == 1)
             tiles.push_back(t);
     st = search(tiles, false, make_and_time, validate, &e, report);
     clear_error();

@@ -495,9 +495,10 @@ def run_ours(args):
 
 OCTREE_SCENES = 6
 OCTREE_FP64_SAMPLE = 4096
-# (fine tile preset, budgets): 8^3 tiles (the learned octree's) for small budgets, the
-# dense pass's 16 x 16 x 8 tiles (a tile then spans 2 x 2 x 1 score blocks) for large ones
-FRONTIER = ((10, (0.04, 0.05, 0.075, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6)),
+# (fine tile preset, budgets): 8^3 tiles (the learned octree's, four per CTA) for small
+# budgets, the dense pass's 16 x 16 x 8 tiles (a tile then spans 2 x 2 x 1 score blocks)
+# for large ones
+FRONTIER = ((13, (0.04, 0.05, 0.075, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6)),
             (3, (0.3, 0.4, 0.5, 0.6, 0.7, 0.8)))
 
 
@@ -581,7 +582,7 @@ def measure_octree(args, dev, frontier: bool = True) -> dict:
     ms, launches = timed(rec, 0.0, args.steps, args.warmup)
     points_raw = []
     for tile, budgets in series:
-        r = rec if tile == 10 else octree.Reconstructor(geo, dev, fine_tile=tile, fine_splits=4)
+        r = rec if tile == 13 else octree.Reconstructor(geo, dev, fine_tile=tile, fine_splits=4)
         for b in budgets:
             q = []
             for rows, amax, d32, occ, f64 in scenes:

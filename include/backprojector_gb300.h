@@ -86,11 +86,14 @@ typedef struct bpgb_options {
     int32_t accum;       /* bpgb_accum */
     uint32_t h_pitch;    /* elements between consecutive H rows (0 = T) */
     float h_scale;       /* result multiplier (FP16/BF16 per-capture scale; 0 = 1) */
-    int32_t tile;        /* tile preset index (-1 = tuned default) */
+    int32_t tile;        /* tile preset index (-1 = tuned default); 10-12: small tiles for
+                            block-sparse passes, 13: four 8^3 tiles per CTA (real rows,
+                            plain sums) */
     int32_t pair_splits; /* CTAs sharing one voxel tile over disjoint pair ranges (0 = auto) */
     int32_t checked;     /* 1 = clamp and count out-of-window bins (tests) */
     uint32_t spin_limit; /* bounded mbarrier waits: polls before giving up (0 = default) */
-    int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..64 (0 = from the preset) */
+    int32_t chunk;       /* FAST: SPAD rows per pipeline stage, 1..64 (0 = from the preset;
+                            preset 13: per tile, a power of two up to 32) */
     int32_t stages;      /* FAST: pipeline depth, 2..8 (0 = from the preset) */
     int32_t unfactored;  /* FAST, lasers x SPADs captures: 0 = per-voxel laser and SPAD legs
                             computed once per block and reused across the other grid

@@ -270,7 +270,7 @@ def test_block_max_and_upsample(cuda):
     assert torch.allclose(fine.cpu(), ref, rtol=1e-5, atol=1e-5)
 
 
-@pytest.mark.parametrize("tile", [10, 11, 12])
+@pytest.mark.parametrize("tile", [10, 11, 12, 13])
 def test_small_tile_presets_vs_oracle(cuda, tile):
     import torch
 
@@ -282,11 +282,12 @@ def test_small_tile_presets_vs_oracle(cuda, tile):
                    algo=capi.ALGO_FAST, tile=tile, checked=1) as p:
         p.execute(dH, dV)
         assert p.check() == 0
-        assert p.info()["threads"] in (96, 160)
+        assert p.info()["threads"] in (96, 160, 288)
     assert oracle.rel_l2(dV.cpu().numpy(), ref) < 5e-3
 
 
-@pytest.mark.parametrize("tile,splits", [(0, 1), (10, 1), (10, 2), (11, 3), (0, 4)])
+@pytest.mark.parametrize("tile,splits", [(0, 1), (10, 1), (10, 2), (11, 3), (0, 4), (13, 1),
+                                         (13, 3)])
 def test_tile_list_execution_matches_dense(cuda, tile, splits):
     import torch
 
@@ -332,13 +333,15 @@ def test_tile_list_execution_matches_dense(cuda, tile, splits):
     assert np.all(mask[sc])
 
 
-def test_octree_pipeline_limits(cuda):
+@pytest.mark.parametrize("fine_tile", [10, 13])
+def test_octree_pipeline_limits(cuda, fine_tile):
     """Untrained model: p_lo = 0 computes every block (equals dense); p_lo -> 1 computes
-    none (the trilinear fill of the coarse pass)."""
+    none (the trilinear fill of the coarse pass).  One 8^3 tile per CTA (preset 10) and
+    four (preset 13)."""
     import torch
 
     geo = octree.OctreeGeometry.of("octree_256", small=True)
-    rec = octree.Reconstructor(geo, cuda, fine_tile=10)
+    rec = octree.Reconstructor(geo, cuda, fine_tile=fine_tile)
     model = octree.OccupancyCNN(cuda, seed=1)
     pts, alb = octree.scene(geo, 7)
     rec.render(pts, alb)
@@ -440,6 +443,47 @@ def test_native_octree_matches_python_pipeline(cuda):
     assert recall >= 0.99
     assert 0 < n_sel < 0.15 * info["tiles"]
     rec.close()
+
+
+@pytest.mark.parametrize("splits,h_dtype", [(1, capi.DTYPE_F32), (2, capi.DTYPE_F16),
+                                             (3, capi.DTYPE_BF16)])
+def test_grouped_tile_list_ragged(cuda, splits, h_dtype):
+    """Four 8^3 tiles per CTA (preset 13) over a list whose length is no multiple of four:
+    a count above max_tiles is clamped to it, an entry outside the volume is skipped, the
+    entries past max_tiles stay untouched, and every listed tile equals the dense pass of
+    the same plan bit for bit (FP32, FP16 and BF16 rows)."""
+    import torch
+
+    c = synthetic.make_capture("octree_256", seed=7, small=True)
+    H = torch.from_numpy(c.H).to(cuda)
+    opt = dict(algo=capi.ALGO_FAST, tile=13, pair_splits=splits, h_dtype=h_dtype)
+    if h_dtype == capi.DTYPE_F16:
+        H = H.half()
+    elif h_dtype == capi.DTYPE_BF16:
+        H = H.bfloat16()
+    N = tuple(int(v) for v in c.voxels_per_side)
+    dense = torch.empty(N, device=cuda)
+    with capi.Plan(c.pairs, c.T, N, c.zero, c.inc, c.t0, c.deltaT, **opt) as p:
+        info = p.info()
+        assert info["threads"] == 288 and list(info["tile"]) == [8, 8, 8]
+        p.execute(H, dense)
+        nt = [-(-n // 8) for n in N]
+        ntiles = int(np.prod(nt))
+        ids = [5, ntiles + 3, 17, 2, ntiles - 1, 40, 41, 9, 11, 30]
+        lst = torch.tensor(ids, dtype=torch.int32, device=cuda)
+        cnt = torch.tensor([12], dtype=torch.int32, device=cuda)
+        out = torch.full(N, float("nan"), device=cuda)
+        p.execute_tiles(H, out, lst, cnt, 9)
+        assert p.check() == 0
+    o, d = out.cpu().numpy(), dense.cpu().numpy()
+    mask = np.zeros(N, bool)
+    for t in ids[:9]:
+        if t >= ntiles:
+            continue
+        tz, tx, ty = t % nt[2], (t // nt[2]) % nt[0], t // (nt[2] * nt[0])
+        mask[tx * 8:(tx + 1) * 8, ty * 8:(ty + 1) * 8, tz * 8:(tz + 1) * 8] = True
+    assert np.array_equal(~np.isnan(o), mask)
+    assert np.array_equal(o[mask], d[mask])
 
 
 @pytest.mark.parametrize("h_dtype", [capi.DTYPE_C64, capi.DTYPE_C32])
@@ -586,14 +630,15 @@ def test_block_detail_vs_torch(cuda):
     assert torch.allclose(got.reshape(-1)[mask], ref.reshape(-1)[mask], rtol=1e-4, atol=1e-6)
 
 
-def test_budgeted_reconstruction_limits(cuda):
+@pytest.mark.parametrize("fine_tile", [10, 13])
+def test_budgeted_reconstruction_limits(cuda, fine_tile):
     """budget = 1 computes every block (equal to the dense pass bit for bit); a small
     budget computes at least the CNN's blocks and fills the rest from the 64^3-style
     second pass."""
     import torch
 
     geo = octree.OctreeGeometry.of("octree_256", small=True)
-    rec = octree.Reconstructor(geo, cuda, fine_tile=10)
+    rec = octree.Reconstructor(geo, cuda, fine_tile=fine_tile)
     model = octree.OccupancyCNN(cuda, seed=1)
     rec.render(*octree.scene(geo, 9))
     dense = rec.dense().clone()
