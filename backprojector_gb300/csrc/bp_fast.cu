@@ -33,9 +33,8 @@
 //   * Stages are handed over with mbarriers (full: TMA bytes + producer arrive; empty:
 //     one arrive per consumer warp; the producer sleeps briefly between its polls, so
 //     that they take no issue slots from the consumers).  Every wait is bounded; a wait
-//     that gives up sets
-//     an error counter the host reads (bpgb_plan_check) and the CTA drains its own
-//     in-flight copies before returning.
+//     that gives up sets an error counter the host reads (bpgb_plan_check) and the CTA
+//     drains its own in-flight copies before returning.
 //
 // Numerics: FP32 geometry relative to the tile centre, rsqrt.approx; FP32 or Kahan-
 // folded chunk sums.  Rounding is round-half-even instead of the reference's half-away
