@@ -161,21 +161,54 @@ __device__ __forceinline__ void box_bounds(const FastArgs &a, const TileGeo &g, 
     dmax = sqrtf(s1);
 }
 
-// Row record of SPAD entry G (frame position, row constant Cs) for a tile and laser Lt:
-// e[a] = SPAD coordinate a relative to the tile centre in bin units, ew = Cs - lo;
-// returns lo, the window's first bin, aligned down to a.align.
-__device__ __forceinline__ int32_t row_record(const FastArgs &a, const TileGeo &g, float4 G,
-                                              float4 Lt, float e[3], float &ew) {
-    float dmin, dmax, lmin, lmax;
-    box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
-    box_bounds(a, g, Lt.x, Lt.y, Lt.z, lmin, lmax);
-    const float bmin = __fmaf_rn(a.sb, dmin, G.w) + __fmaf_rn(a.sa, lmin, Lt.w);
-    int32_t lo = (int32_t)floorf(bmin - kMargin);
-    const int32_t al = (int32_t)a.align;
-    lo -= ((lo % al) + al) % al;
+// lo rounded down to a multiple of al, a power of two (the TMA alignment in elements).
+__device__ __forceinline__ int32_t align_down(int32_t lo, uint32_t al) {
+    return lo & -(int32_t)al;
+}
+
+// A tile's box of voxel centres and its centre in frame coordinates (metres), formed once
+// per tile for the producer's row records (the same products box_bounds forms).
+struct TileBox {
+    float lo[3], hi[3], ch[3];
+};
+
+__device__ __forceinline__ void tile_box(const FastArgs &a, const TileGeo &g, TileBox &b) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        b.lo[k] = __fmul_rn((float)g.org[k], a.h[k]);
+        b.hi[k] = __fmul_rn((float)(g.org[k] + a.tdim[k] - 1), a.h[k]);
+        b.ch[k] = __fmul_rn(g.ctr[k], a.h[k]);
+    }
+}
+
+// box_bounds' minimum distance, from the precomputed box.
+__device__ __forceinline__ float box_dmin(const TileBox &b, float px, float py, float pz) {
+    const float p[3] = {px, py, pz};
+    float s0 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float d0 = p[k] - fminf(fmaxf(p[k], b.lo[k]), b.hi[k]);
+        s0 = __fmaf_rn(d0, d0, s0);
+    }
+    return sqrtf(s0);
+}
+
+// The laser's part of a tile's window start: sa x (min distance to the box) + Lt.w; one per
+// (tile, laser), shared by every SPAD row of that laser.
+__device__ __forceinline__ float laser_term(const FastArgs &a, const TileBox &b, float4 Lt) {
+    return __fmaf_rn(a.sa, box_dmin(b, Lt.x, Lt.y, Lt.z), Lt.w);
+}
+
+// Row record of SPAD entry G (frame position, row constant Cs) for a tile (box b) and the
+// laser's laser_term lt: e[a] = SPAD coordinate a relative to the tile centre in bin units,
+// ew = Cs - lo; returns lo, the window's first bin, aligned down to a.align.
+__device__ __forceinline__ int32_t row_record(const FastArgs &a, const TileBox &b, float4 G,
+                                              float lt, float e[3], float &ew) {
+    const float bmin = __fmaf_rn(a.sb, box_dmin(b, G.x, G.y, G.z), G.w) + lt;
+    const int32_t lo = align_down((int32_t)floorf(bmin - kMargin), a.align);
     const float gp[3] = {G.x, G.y, G.z};
 #pragma unroll
-    for (int k = 0; k < 3; k++) e[k] = __fmul_rn(gp[k] - __fmul_rn(g.ctr[k], a.h[k]), a.sb);
+    for (int k = 0; k < 3; k++) e[k] = __fmul_rn(gp[k] - b.ch[k], a.sb);
     ew = G.w - (float)lo;
     return lo;
 }
@@ -486,26 +519,39 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
 
     if (warp == 0) {
         // ---------------- producer ----------------
-        // GROUPED: entry lane + 32 q of a stage is row (lane + 32 q) % chunk of tile
-        // (lane + 32 q) / chunk of the group, whose geometry (and whether it exists) the
-        // producer keeps in shared memory for the unit
+        // The tile's box, and the laser's part of every window start (laser_term) while
+        // the laser stays the same.  GROUPED: entry lane + 32 q of a stage is row
+        // (lane + 32 q) % chunk of tile (lane + 32 q) / chunk of the group; the tiles'
+        // boxes, laser terms and whether they exist are kept in shared memory.
         uint32_t nvalid = 1;  // tiles of the group that exist
-        const TileGeo *geo = nullptr;
-        const uint32_t *geo_ok = nullptr;
+        TileBox box;
+        float lt = 0.0f;
+        uint32_t cur_l = ~0u;
+        TileBox *box_g = nullptr;
+        float *lt_g = nullptr;
+        const uint32_t *ok_g = nullptr;
         uint32_t cshift = 0;
         if constexpr (GROUPED) {
-            __shared__ TileGeo geo_s[kMaxGroups];
+            __shared__ TileBox box_s[kMaxGroups];
+            __shared__ float lt_s[kMaxGroups];
             __shared__ uint32_t ok_s[kMaxGroups];
             if (lane < kMaxGroups) {
                 void *unused;
                 ok_s[lane] = lane < a.groups && group_tile<PairT>(a, out, t0, lane, tile, unused);
-                if (ok_s[lane]) tile_of_block(a, tile, geo_s[lane]);
+                if (ok_s[lane]) {
+                    TileGeo gt;
+                    tile_of_block(a, tile, gt);
+                    tile_box(a, gt, box_s[lane]);
+                }
             }
             __syncwarp();
             nvalid = ok_s[0] + ok_s[1] + ok_s[2] + ok_s[3];
-            geo = geo_s;
-            geo_ok = ok_s;
+            box_g = box_s;
+            lt_g = lt_s;
+            ok_g = ok_s;
             cshift = __ffs(a.chunk) - 1;  // chunk = 2^cshift
+        } else {
+            tile_box(a, g, box);
         }
         // stage / round of the ring and (laser, chunk) of the item advance by counting: no
         // 64-bit division per stage
@@ -534,6 +580,17 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
                 step = i;
                 return false;
             }
+            if (l != cur_l) {  // a new laser: its part of the window starts
+                const float4 Lt = lasers[l];
+                if constexpr (GROUPED) {
+                    __syncwarp();  // every lane is done with the previous laser's terms
+                    if (lane < kMaxGroups && ok_g[lane]) lt_g[lane] = laser_term(a, box_g[lane], Lt);
+                    __syncwarp();
+                } else {
+                    lt = laser_term(a, box, Lt);
+                }
+                cur_l = l;
+            }
             const uint64_t s0 = (uint64_t)c * a.chunk;
             const uint32_t nrows =
                 (uint32_t)(a.S - s0 < (uint64_t)a.chunk ? a.S - s0 : (uint64_t)a.chunk);
@@ -548,11 +605,10 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
 #pragma unroll 1
                 for (uint32_t q = 0; q < kLane; q++) {
                     const uint32_t e = lane + 32 * q, r = e & (a.chunk - 1), gi = e >> cshift;
-                    if (r < nrows && gi < kMaxGroups && geo_ok[gi]) {
+                    if (r < nrows && gi < kMaxGroups && ok_g[gi]) {
                         const float4 G = spads[s0 + r];
-                        const float4 Lt = lasers[l];
                         float ev[3], ew;
-                        const int32_t lo = row_record(a, geo[gi], G, Lt, ev, ew);
+                        const int32_t lo = row_record(a, box_g[gi], G, lt_g[gi], ev, ew);
                         const float ek = sel3(ev[0], ev[1], ev[2], a.kax);
                         table[2 * e] = make_float4(sel3(ev[0], ev[1], ev[2], a.oax0),
                                                    sel3(ev[0], ev[1], ev[2], a.oax1), ew, ew);
@@ -572,9 +628,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
                     const uint32_t e = lane + 32 * q, r = e;
                     if (r < nrows) {
                         const float4 G = spads[s0 + r];
-                        const float4 Lt = lasers[l];
                         float ev[3], ew;
-                        lo[q] = row_record(a, g, G, Lt, ev, ew);
+                        lo[q] = row_record(a, box, G, lt, ev, ew);
                         const float ek = sel3(ev[0], ev[1], ev[2], a.kax);
                         table[2 * e] = make_float4(sel3(ev[0], ev[1], ev[2], a.oax0),
                                                    sel3(ev[0], ev[1], ev[2], a.oax1), ew, ew);
@@ -881,7 +936,7 @@ __device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *
                 float dmin, dmax;
                 box_bounds(a, g, Lt.x, Lt.y, Lt.z, dmin, dmax);
                 lo_l = (int32_t)floorf(__fmaf_rn(a.sa, dmin, Lt.w) - kMargin);
-                lo_l -= ((lo_l % al) + al) % al;
+                lo_l = align_down(lo_l, al);
                 const float lp[3] = {Lt.x, Lt.y, Lt.z};
                 float e[3];
 #pragma unroll
@@ -896,7 +951,7 @@ __device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *
                 float dmin, dmax;
                 box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
                 lo_s = (int32_t)floorf(__fmaf_rn(a.sb, dmin, G.w));
-                lo_s -= ((lo_s % al) + al) % al;
+                lo_s = align_down(lo_s, al);
                 const float gp[3] = {G.x, G.y, G.z};
                 float e[3];
 #pragma unroll
@@ -1251,9 +1306,9 @@ __global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
             box_bounds(a, g, Lt.x, Lt.y, Lt.z, lmin, lmax);
             box_bounds(a, g, G.x, G.y, G.z, dmin, dmax);
             int32_t lo_l = (int32_t)floorf(__fmaf_rn(a.sa, lmin, Lt.w) - kMargin);
-            lo_l -= ((lo_l % al) + al) % al;
+            lo_l = align_down(lo_l, al);
             int32_t lo_s = (int32_t)floorf(__fmaf_rn(a.sb, dmin, G.w));
-            lo_s -= ((lo_s % al) + al) % al;
+            lo_s = align_down(lo_s, al);
             const float v[3] = {rel_coord(a, g, 0, idx[0]), rel_coord(a, g, 1, idx[1]),
                                 rel_coord(a, g, 2, idx[2])};
             auto leg = [&](float4 P4, float sc, float c) {
@@ -1276,7 +1331,9 @@ __global__ void bp_fast_bins_kernel(const float4 *__restrict__ spads,
             continue;
         }
         float e[3], ew;
-        const int32_t lo = row_record(a, g, spads[s], Lt, e, ew);
+        TileBox tb;
+        tile_box(a, g, tb);
+        const int32_t lo = row_record(a, tb, spads[s], laser_term(a, tb, Lt), e, ew);
         const float A = laser_leg(a, idx, Lt);
         const float v0 = rel_coord(a, g, a.oax0, sel3(idx[0], idx[1], idx[2], a.oax0));
         const float v1 = rel_coord(a, g, a.oax1, sel3(idx[0], idx[1], idx[2], a.oax1));
