@@ -906,8 +906,8 @@ __device__ __forceinline__ bool fact_unit(const FastArgs &a, const CUtensorMap *
         for (uint32_t n = 0; n < count; n++) {
             const uint64_t i = step0 + n;
             if (round > 0) {
-                bool ok = mbar_wait(smem_addr(&empty_bar[stage]), (uint32_t)(round - 1) & 1,
-                                    a.spin_limit);
+                bool ok = mbar_wait_backoff(smem_addr(&empty_bar[stage]),
+                                            (uint32_t)(round - 1) & 1, a.spin_limit);
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) {
                     if (lane == 0) {
