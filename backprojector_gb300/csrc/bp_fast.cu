@@ -584,7 +584,8 @@ __device__ __forceinline__ bool fast_unit(const FastArgs &a, const CUtensorMap *
                 const float4 Lt = lasers[l];
                 if constexpr (GROUPED) {
                     __syncwarp();  // every lane is done with the previous laser's terms
-                    if (lane < kMaxGroups && ok_g[lane]) lt_g[lane] = laser_term(a, box_g[lane], Lt);
+                    if (lane < kMaxGroups && ok_g[lane])
+                        lt_g[lane] = laser_term(a, box_g[lane], Lt);
                     __syncwarp();
                 } else {
                     lt = laser_term(a, box, Lt);
