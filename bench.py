@@ -472,7 +472,7 @@ def run_ours(args):
         line["stage_ms"] = {"backprojection": bp_ms, "pulse_and_conversion": ms - bp_ms}
     plan.close()
     if args.workload == "octree_256" and not args.no_octree:
-        # the benchmark spec's headline: the learned octree against this dense pass, in the
+        # the headline comparison: the learned octree against this dense pass, in the
         # same process (measure_octree)
         with ClockSampler(local) as oclk:
             m = measure_octree(args, dev)

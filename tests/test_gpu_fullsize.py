@@ -9,8 +9,8 @@ drawn uniformly over each volume (empty space included, not only occupied voxels
   16^2 x 16^2 lasers x SPADs captures) in the persistent batch launches, sampled voxels in
   every capture.
 
-Tolerance: rel-L2 <= 1e-3 on the sampled voxels wherever P >= 1024 (the benchmark spec's
-figure for FP32 arithmetic), FP16-stored rows scored against the oracle on the same
+Tolerance: rel-L2 <= 1e-3 on the sampled voxels wherever P >= 1024 (the accuracy target
+for FP32 arithmetic), FP16-stored rows scored against the oracle on the same
 dequantised rows; mis-binned fraction of (voxel, pair) bins against the FP64 oracle's
 <= 1e-3 on the dense capture.
 """
