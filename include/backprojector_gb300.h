@@ -179,8 +179,10 @@ int bpgb_plan_execute(bpgb_plan plan, const void *d_H, void *d_volume, void *str
 /* Block-sparse form of bpgb_plan_execute (FAST plans): computes only the voxel tiles
  * listed in device memory, d_tile_list[0 .. *d_tile_count), and leaves every other voxel
  * of d_volume untouched.  max_tiles bounds *d_tile_count and sets the launch size
- * (max_tiles x pair_splits CTAs; those past the count exit at once), so the call reads
- * no device value on the host and can be captured in a CUDA graph.  With pair_splits > 1
+ * (max_tiles x pair_splits CTAs, or ceil(max_tiles / 4) x pair_splits with tile preset
+ * 13's four tiles per CTA; those past the count exit at once; list entries outside the
+ * volume are skipped), so the call reads no device value on the host and can be captured
+ * in a CUDA graph.  With pair_splits > 1
  * each listed tile's pairs are split over that many CTAs and a second kernel adds the
  * partial sums in split order, exactly as bpgb_plan_execute does, so the listed voxels
  * equal the full execute's bit for bit.  Tile ids follow the plan's tile grid
